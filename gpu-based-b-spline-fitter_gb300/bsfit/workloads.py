@@ -1,0 +1,323 @@
+"""Seeded synthetic workloads for the B-spline fitter.
+
+The reference publishes no dataset for this path; every input here is
+synthetic, seeded with ``numpy.random.default_rng``. Each workload builds a
+PSF sample stack, turns it into cubic B-spline coefficients with the
+reference's prefilter (``prefilter.bsarray_coeffs``), and draws Poisson ROIs
+from the analytic PSF at seeded emitter positions.
+
+Array conventions (the reference's mex layout, MATLAB column-major):
+- coefficients: numpy C-order shape (..., Z, X, Y), i.e. MATLAB [Y, X, Z, ...]
+  with Y fastest; ``cdims`` lists the MATLAB sizes (Y, X, Z, W, U).
+- ROIs: numpy shape (N, s, s) indexed [roi, jj, ii], i.e. MATLAB [s, s, N];
+  pixel (ii, jj) is ``data[s*jj + ii]``.
+- Parameter 0 (x) moves the PSF along jj (the X axis), parameter 1 (y) along
+  ii (the Y axis); pixel jj of a centred emitter sits at x = jj.
+
+Lateral grid: the reference evaluates pixel jj at knot position
+(s + 1) / 2 - x + jj + (nX - s) / 2 with nX = (coefficient size - 3) and
+takes the spline weights from the fractional part of (s + 1) / 2 - x only
+(CPUmleFit_LM.cpp:2512-2519, CPUsplineLib.cpp:1199-1230). The model is
+continuous in x only when nX - s is even, so the generators use an even
+number of lateral samples (odd nX) for the odd ROI sizes 11, 13, 15 and 17, with
+the PSF centred on sample (nX - 1) / 2.
+"""
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+from . import prefilter
+
+SEED = 1234
+
+
+@dataclass
+class Workload:
+    name: str
+    fittype: int
+    iterations: int
+    coeff: np.ndarray            # float32, C-order (..., Z, X, Y)
+    rois: np.ndarray             # float32 (N, s, s)
+    truth: dict
+    init_p: np.ndarray = None    # float32 shared initP (modes 7 and 8)
+    coeff3: np.ndarray = None    # float32 3D coefficients (mode 8)
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def cdims(self):
+        """MATLAB dimension sizes of the coefficient array (Y, X, Z, ...)."""
+        return tuple(reversed(self.coeff.shape))
+
+    @property
+    def roi_size(self):
+        return self.rois.shape[-1]
+
+    @property
+    def n_fits(self):
+        return self.rois.shape[0]
+
+
+def _rng(stream):
+    return np.random.default_rng([SEED, stream])
+
+
+def _int_gauss(center, sigma, n):
+    """Pixel-integrated unit Gaussian on pixels 0..n-1; center/sigma shape (N,)."""
+    edges = np.arange(n + 1, dtype=np.float64)[None, :] - 0.5
+    u = (edges - center[:, None]) / (math.sqrt(2.0) * sigma[:, None])
+    cdf = 0.5 * (1.0 + _erf(u))
+    return np.diff(cdf, axis=1)
+
+
+def _erf(x):
+    try:
+        from scipy.special import erf
+        return erf(x)
+    except ImportError:  # pragma: no cover - the GPU machine has scipy
+        return np.vectorize(math.erf)(x)
+
+
+def astig_sigmas(z_nm, sigma0=1.3):
+    """sigma_x, sigma_y (px) of the astigmatic PSF at z (nm)."""
+    z = np.asarray(z_nm, dtype=np.float64)
+    sx = sigma0 * np.sqrt(1.0 + ((z - 200.0) / 400.0) ** 2)
+    sy = sigma0 * np.sqrt(1.0 + ((z + 200.0) / 400.0) ** 2)
+    return sx, sy
+
+
+# ---------------------------------------------------------------------------
+# 3D astigmatic model (fit type 6)
+
+Z_STEP_NM = 20.0
+
+
+def psf3d_samples(n_lat=26, z_lo=-600.0, z_hi=600.0, sigma0=1.3):
+    """PSF stack (Z, X, Y) at 1 px lateral pitch, centre on sample (n_lat-2)/2."""
+    nz = int(round((z_hi - z_lo) / Z_STEP_NM)) + 1
+    z = z_lo + Z_STEP_NM * np.arange(nz)
+    c = (n_lat - 2) / 2.0
+    sx, sy = astig_sigmas(z, sigma0)
+    gx = _int_gauss(np.full(nz, c), sx, n_lat)  # (Z, X)
+    gy = _int_gauss(np.full(nz, c), sy, n_lat)  # (Z, Y)
+    return gx[:, :, None] * gy[:, None, :], z
+
+
+def z_to_param(z_nm, z_lo=-600.0):
+    """Fit parameter z (padded knot units) for a physical z in nm."""
+    return (np.asarray(z_nm) - z_lo) / Z_STEP_NM + 1.0
+
+
+def param_to_z(p, z_lo=-600.0):
+    return (np.asarray(p) - 1.0) * Z_STEP_NM + z_lo
+
+
+def _coeff_f32(samples):
+    return np.ascontiguousarray(prefilter.bsarray_coeffs(samples).astype(np.float32))
+
+
+_COEFF_CACHE = {}
+
+
+def coeff3d(n_lat=26, sigma0=1.3):
+    key = ("3d", n_lat, sigma0)
+    if key not in _COEFF_CACHE:
+        s, _ = psf3d_samples(n_lat, sigma0=sigma0)
+        _COEFF_CACHE[key] = _coeff_f32(s)
+    return _COEFF_CACHE[key]
+
+
+def rois3d(n, s, rng, sigma0=1.3, xy_spread=1.5, z_range=600.0, n_lo=1000.0, n_hi=5000.0,
+           bg_lo=5.0, bg_hi=20.0):
+    """Poisson ROIs of the astigmatic PSF; returns (rois, truth)."""
+    cx = (s - 1) / 2.0
+    x = cx + rng.uniform(-xy_spread, xy_spread, n)
+    y = cx + rng.uniform(-xy_spread, xy_spread, n)
+    z = rng.uniform(-z_range, z_range, n)
+    photons = np.exp(rng.uniform(math.log(n_lo), math.log(n_hi), n))
+    bg = rng.uniform(bg_lo, bg_hi, n)
+    sx, sy = astig_sigmas(z, sigma0)
+    gx = _int_gauss(x, sx, s)   # along jj
+    gy = _int_gauss(y, sy, s)   # along ii
+    model = bg[:, None, None] + photons[:, None, None] * gx[:, :, None] * gy[:, None, :]
+    rois = rng.poisson(model).astype(np.float32)
+    truth = dict(x=x, y=y, z_nm=z, z=z_to_param(z), N=photons, bg=bg)
+    return rois, truth
+
+
+def workload_3d(n=10000, s=13, iterations=30, stream=1):
+    """Plain 3D astigmatic fit: n ROIs of s x s, 30 LM iterations."""
+    rng = _rng(stream)
+    rois, truth = rois3d(n, s, rng)
+    return Workload(f"3d_{s}px", 6, iterations, coeff3d(), rois, truth)
+
+
+def workload_3d_mixed(n=1_000_000, sizes=(11, 13, 17), ratio=(1, 2, 1), iterations=30,
+                      stream=2):
+    """Batched 3D: ROIs of several sizes (ratio 1:2:1); one Workload per size."""
+    rng = _rng(stream)
+    tot = sum(ratio)
+    counts = [n * r // tot for r in ratio]
+    counts[sizes.index(13) if 13 in sizes else 0] += n - sum(counts)
+    out = []
+    for s, c in zip(sizes, counts):
+        rois, truth = rois3d(c, s, rng)
+        out.append(Workload(f"3d_{s}px", 6, iterations, coeff3d(), rois, truth))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# 4D colour model (fit type 7)
+
+def color_sigma(lam):
+    """Base sigma (px) for colour coordinate lam in [0, 1]."""
+    return 1.2 + 0.25 * np.asarray(lam, dtype=np.float64)
+
+
+def psf4d_samples(n_lat=26, z_lo=-600.0, z_hi=600.0):
+    """(W, Z, X, Y) stack; the colour axis is end-padded like the reference's
+    colour demo (bspline_based_color_classification_v3.m:19-25): samples
+    [l0, l0, l1/3, l2/3, l1, l1, l1], so colour lam sits at w = 2 + 3 lam."""
+    lam_knots = np.array([0.0, 0.0, 1 / 3, 2 / 3, 1.0, 1.0, 1.0])
+    stacks = []
+    for lam in lam_knots:
+        s3, z = psf3d_samples(n_lat, z_lo, z_hi, sigma0=float(color_sigma(lam)))
+        stacks.append(s3)
+    return np.stack(stacks, axis=0), z
+
+
+def lam_to_w(lam):
+    return 2.0 + 3.0 * np.asarray(lam)
+
+
+def coeff4d(n_lat=26):
+    key = ("4d", n_lat)
+    if key not in _COEFF_CACHE:
+        s, _ = psf4d_samples(n_lat)
+        _COEFF_CACHE[key] = _coeff_f32(s)
+    return _COEFF_CACHE[key]
+
+
+def workload_4d(n=500_000, sizes=(13, 15), iterations=60, stream=3):
+    """3D + colour: ROIs of 13 and 15 px (half each); one Workload per size."""
+    rng = _rng(stream)
+    out = []
+    counts = [n // len(sizes)] * len(sizes)
+    counts[0] += n - sum(counts)
+    for s, c in zip(sizes, counts):
+        cx = (s - 1) / 2.0
+        x = cx + rng.uniform(-1.5, 1.5, c)
+        y = cx + rng.uniform(-1.5, 1.5, c)
+        z = rng.uniform(-600.0, 600.0, c)
+        lam = rng.uniform(0.0, 1.0, c)
+        photons = np.exp(rng.uniform(math.log(800.0), math.log(4000.0), c))
+        bg = rng.uniform(5.0, 15.0, c)
+        sx, sy = astig_sigmas(z, 1.0)
+        sc = color_sigma(lam)
+        gx = _int_gauss(x, sx * sc, s)
+        gy = _int_gauss(y, sy * sc, s)
+        model = bg[:, None, None] + photons[:, None, None] * gx[:, :, None] * gy[:, None, :]
+        rois = rng.poisson(model).astype(np.float32)
+        truth = dict(x=x, y=y, z_nm=z, z=z_to_param(z), lam=lam, w=lam_to_w(lam), N=photons, bg=bg)
+        init_p = np.array([z_to_param(0.0), lam_to_w(0.5)], dtype=np.float32)
+        out.append(Workload(f"4d_{s}px", 7, iterations, coeff4d(), rois, truth, init_p=init_p))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# 5D orientation model (fit type 8)
+
+N_AZ = 18      # azimuth samples per period (20 deg)
+N_POL = 9      # polar samples
+POL_STEP = 10.0
+
+
+def dipole_lobes(x, y, z_nm, phi, theta, s):
+    """Three astigmatic lobes weighted by the dipole orientation.
+
+    Lobe weights sin^2(t)cos^2(p), sin^2(t)sin^2(p), cos^2(t); every lobe is
+    shifted laterally by 0.4 px * (sin t cos p, sin t sin p)."""
+    st, ct = np.sin(theta), np.cos(theta)
+    sp, cp = np.sin(phi), np.cos(phi)
+    w = [st ** 2 * cp ** 2, st ** 2 * sp ** 2, ct ** 2]
+    dx = 0.4 * st * cp
+    dy = 0.4 * st * sp
+    sx, sy = astig_sigmas(z_nm, 1.3)
+    sig = [(sx, sy), (sy, sx), (0.5 * (sx + sy) * 1.1, 0.5 * (sx + sy) * 1.1)]
+    out = 0.0
+    for wi, (gsx, gsy) in zip(w, sig):
+        gx = _int_gauss(x + dx, gsx, s)
+        gy = _int_gauss(y + dy, gsy, s)
+        out = out + wi[:, None, None] * gx[:, :, None] * gy[:, None, :]
+    return out
+
+
+def psf5d_samples(n_lat=34, z_lo=-400.0, z_hi=400.0, n_az=N_AZ, n_pol=N_POL):
+    """(U, W, Z, X, Y) stack over one azimuth period and the polar grid."""
+    nz = int(round((z_hi - z_lo) / Z_STEP_NM)) + 1
+    zs = z_lo + Z_STEP_NM * np.arange(nz)
+    c = (n_lat - 2) / 2.0
+    out = np.zeros((n_pol, n_az, nz, n_lat, n_lat))
+    for iu in range(n_pol):
+        th = np.deg2rad(POL_STEP * iu)
+        for iw in range(n_az):
+            ph = 2 * np.pi * iw / n_az
+            # lobes at every z of the grid, emitter at the sample centre
+            lob = dipole_lobes(np.full(nz, c), np.full(nz, c), zs, np.full(nz, ph),
+                               np.full(nz, th), n_lat)
+            out[iu, iw] = lob
+    return out, zs
+
+
+def coeff5d(n_lat=34, z_lo=-400.0, z_hi=400.0, n_az=N_AZ, n_pol=N_POL):
+    """5D coefficients (U, W, Z, X, Y) and the orientation-averaged 3D ones.
+
+    The azimuth axis W is periodic: the fitter wraps w into (1, nW - 1] with
+    period nW - 2 (CPUmleFit_LM.cpp:3436-3443), so the coefficients along W are
+    the periodic interpolating spline laid out as c[m] = c_per[(m - 2) mod n_az]
+    for m = 0 .. n_az + 4 (nW = n_az + 2). The polar axis U uses the mirror
+    prefilter."""
+    key = ("5d", n_lat, z_lo, z_hi, n_az, n_pol)
+    if key not in _COEFF_CACHE:
+        s, _ = psf5d_samples(n_lat, z_lo, z_hi, n_az, n_pol)
+        c = s
+        for ax in (2, 3, 4):           # Z, X, Y: mirror prefilter
+            c = prefilter.filter_axis(c, ax)
+        c = prefilter.filter_axis(c, 0)  # U: mirror
+        c = prefilter.filter_axis_periodic(c, 1)  # W: periodic
+        c = prefilter.mirror_pad(c, axes=(0, 2, 3, 4))
+        m = np.arange(n_az + 5)
+        c = np.take(c, (m - 2) % n_az, axis=1)
+        c5 = np.ascontiguousarray(c.astype(np.float32))
+        s3 = s.mean(axis=(0, 1))
+        c3 = _coeff_f32(s3)
+        _COEFF_CACHE[key] = (c5, c3)
+    return _COEFF_CACHE[key]
+
+
+def phi_to_w(phi):
+    return np.asarray(phi) / (2 * np.pi / N_AZ) + 2.0
+
+
+def theta_to_u(theta):
+    return np.rad2deg(np.asarray(theta)) / POL_STEP + 1.0
+
+
+def workload_5d(n=100_000, s=17, iterations=60, stream=5):
+    rng = _rng(stream)
+    c5, c3 = coeff5d()
+    cx = (s - 1) / 2.0
+    x = cx + rng.uniform(-1.0, 1.0, n)
+    y = cx + rng.uniform(-1.0, 1.0, n)
+    z = rng.uniform(-300.0, 300.0, n)
+    phi = rng.uniform(0.0, 2 * np.pi, n)
+    theta = np.deg2rad(rng.uniform(10.0, 70.0, n))
+    photons = rng.uniform(2000.0, 8000.0, n)
+    bg = rng.uniform(5.0, 20.0, n)
+    model = bg[:, None, None] + photons[:, None, None] * dipole_lobes(x, y, z, phi, theta, s)
+    rois = rng.poisson(model).astype(np.float32)
+    truth = dict(x=x, y=y, z_nm=z, z=z_to_param(z, -400.0), phi=phi, w=phi_to_w(phi),
+                 theta=theta, u=theta_to_u(theta), N=photons, bg=bg, g2=np.ones(n))
+    init_p = np.array([z_to_param(0.0, -400.0), phi_to_w(np.pi), theta_to_u(np.deg2rad(40.0)),
+                       0.7], dtype=np.float32)
+    return Workload(f"5d_{s}px", 8, iterations, c5, rois, truth, init_p=init_p, coeff3=c3)

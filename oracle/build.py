@@ -1,0 +1,45 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+- ``liboracle.so``: the CPU restatement in ``bsfit_oracle.cpp``, built on
+  every machine (this container and the GPU machine).
+- ``_ref/libref_f32.so`` / ``_ref/libref_f64.so``: the reference's own CPU
+  fitter compiled from its sources by ``build_ref.sh``, only where the reference
+  sources exist (not on the GPU machine).
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REFERENCE_ROOT = os.environ.get("BSFIT_REFERENCE_ROOT", "/root/reference")
+
+
+def build_oracle(force=False):
+    src = os.path.join(HERE, "bsfit_oracle.cpp")
+    if (not force and os.path.exists(ORACLE_SO)
+            and os.path.getmtime(ORACLE_SO) >= os.path.getmtime(src)):
+        return ORACLE_SO
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC",
+           "-o", ORACLE_SO, src]
+    subprocess.run(cmd, check=True)
+    return ORACLE_SO
+
+
+def build_reference(force=False):
+    """Compile the reference CPU fitter when its sources are present."""
+    src = os.path.join(REFERENCE_ROOT, "MultiD_bspline", "visual code",
+                       "CPUmleFit_LM", "CPUmleFit_LM.cpp")
+    if not os.path.exists(src):
+        return None
+    out = os.path.join(REF_DIR, "libref_f32.so")
+    if not force and os.path.exists(out) and os.path.exists(os.path.join(REF_DIR, "libref_f64.so")):
+        return REF_DIR
+    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True)
+    return REF_DIR
+
+
+if __name__ == "__main__":
+    print(build_oracle(force="--force" in sys.argv))
+    print(build_reference(force="--force" in sys.argv))

@@ -1,0 +1,40 @@
+#!/usr/bin/env bash
+# Builds the reference's own CPU B-spline fitter from its sources where they lie
+# (read-only) into oracle/_ref/, as the checker for the oracle restatement:
+#   oracle/_ref/libref_f32.so  FP32, as shipped
+#   oracle/_ref/libref_f64.so  the same sources with float promoted to double
+# Only the three fitter sources are compiled (not erf.cpp, which the reference's
+# own project does not build, nor the mex driver, which needs MATLAB).
+# -fno-stack-protector: the 8-parameter solver kernel_luEvaluate5D declares
+# `float y[7]` and writes y[7] (CPUsplineLib.cpp:17-27); without the flag the
+# canary check aborts. The stray element lands in the array's alignment padding.
+# Usage: oracle/build_ref.sh [reference root]   (default /root/reference)
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${1:-/root/reference}"
+SRC="$REF/MultiD_bspline/visual code/CPUmleFit_LM"
+OUT="$HERE/_ref"
+if [ ! -f "$SRC/CPUmleFit_LM.cpp" ]; then
+  echo "reference sources not found under $SRC; oracle/_ref not built" >&2
+  exit 3
+fi
+mkdir -p "$OUT"
+CXX="${CXX:-g++}"
+FLAGS=(-O2 -fPIC -ffp-contract=off -fno-stack-protector -w -I "$HERE/ref_shim" -I "$SRC" -include "$HERE/ref_shim/prelude.h")
+for variant in f32 f64; do
+  extra=()
+  if [ "$variant" = f64 ]; then extra=(-DBSFIT_REF_PROMOTE_DOUBLE); fi
+  objs=()
+  for f in CPUmleFit_LM.cpp CPUsplineLib.cpp CPUgaussLib.cpp; do
+    o="$OUT/${f%.cpp}_$variant.o"
+    "$CXX" "${FLAGS[@]}" "${extra[@]}" -c "$SRC/$f" -o "$o" &
+    objs+=("$o")
+  done
+  o="$OUT/ref_entry_$variant.o"
+  "$CXX" "${FLAGS[@]}" "${extra[@]}" -c "$HERE/ref_shim/ref_entry.cpp" -o "$o" &
+  objs+=("$o")
+  wait
+  "$CXX" -shared -Wl,--no-undefined -o "$OUT/libref_$variant.so" "${objs[@]}" -lm
+  rm -f "${objs[@]}"
+done
+echo "built $OUT/libref_f32.so $OUT/libref_f64.so"

@@ -1,0 +1,112 @@
+"""ctypes bindings for the oracle libraries (test infrastructure only).
+
+``Oracle`` wraps ``liboracle.so`` (the restatement in ``bsfit_oracle.cpp``);
+``ReferenceOracle`` wraps ``_ref/libref_{f32,f64}.so`` (the reference's CPU
+fitter built by ``build_ref.sh``). Both expose the same ``fit`` call, shaped
+like the reference mex: ``fit(rois, fittype, iterations, coeff, init_p,
+coeff3, precision)`` -> (P, CRLB, LL) with P of shape (N, NV + 1) (last column
+= iterations), CRLB (N, NV), LL (N,).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+NV = {6: 5, 7: 6, 8: 8}
+
+_fp = ctypes.POINTER(ctypes.c_float)
+_dp = ctypes.POINTER(ctypes.c_double)
+_i = ctypes.c_int
+
+
+def _ptr(a, dt):
+    return a.ctypes.data_as(_fp if dt == np.float32 else _dp)
+
+
+class _Base:
+    def _call(self, fn_name, dt, rois, fittype, iterations, coeff, init_p, coeff3, threads):
+        rois = np.ascontiguousarray(rois, dtype=dt)
+        if rois.ndim == 2:
+            rois = rois[None]
+        n, s = rois.shape[0], rois.shape[-1]
+        coeff = np.ascontiguousarray(coeff, dtype=dt)
+        dims = list(reversed(coeff.shape))
+        nv = NV[fittype]
+        P = np.zeros((nv + 1, n), dtype=dt)
+        C = np.zeros((nv, n), dtype=dt)
+        L = np.zeros(n, dtype=dt)
+        fn = getattr(self.lib(dt), fn_name)
+        args = [_ptr(rois, dt), _ptr(coeff, dt)]
+        if fittype == 8:
+            c3 = np.ascontiguousarray(coeff3, dtype=dt)
+            args.append(_ptr(c3, dt))
+        args += [_i(d) for d in dims]
+        args += [_i(s), _i(iterations)]
+        keep = []
+        if fittype in (7, 8):
+            ip = np.ascontiguousarray(init_p, dtype=dt)
+            keep.append(ip)
+            args.append(_ptr(ip, dt))
+        args += [_i(n), _ptr(P, dt), _ptr(C, dt), _ptr(L, dt)]
+        if threads is not None:
+            args.append(_i(threads))
+        fn(*args)
+        return P.T.copy(), C.T.copy(), L
+
+
+class Oracle(_Base):
+    """The CPU restatement (``liboracle.so``), FP32 or FP64."""
+
+    def __init__(self, path=None):
+        path = path or _build.build_oracle()
+        self._lib = ctypes.CDLL(path)
+        for fn in ("oracle_fit6_f32", "oracle_fit6_f64", "oracle_fit7_f32", "oracle_fit7_f64",
+                   "oracle_fit8_f32", "oracle_fit8_f64"):
+            getattr(self._lib, fn).restype = None
+        self._lib.oracle_eval_bspline_f32.restype = ctypes.c_float
+        self._lib.oracle_eval_bspline_f32.argtypes = [ctypes.c_float, ctypes.c_int]
+        self._lib.oracle_eval_bspline_f64.restype = ctypes.c_double
+        self._lib.oracle_eval_bspline_f64.argtypes = [ctypes.c_double, ctypes.c_int]
+
+    def lib(self, dt):
+        return self._lib
+
+    def fit(self, rois, fittype, iterations, coeff, init_p=None, coeff3=None, precision="f32",
+            threads=1):
+        dt = np.float32 if precision == "f32" else np.float64
+        return self._call(f"oracle_fit{fittype}_{precision}", dt, rois, fittype, iterations, coeff,
+                          init_p, coeff3, threads)
+
+    def eval_bspline(self, x, deg, precision="f32"):
+        fn = self._lib.oracle_eval_bspline_f32 if precision == "f32" else self._lib.oracle_eval_bspline_f64
+        return fn(x, deg)
+
+
+def reference_available():
+    return all(os.path.exists(os.path.join(_build.REF_DIR, f"libref_{p}.so")) for p in ("f32", "f64"))
+
+
+class ReferenceOracle(_Base):
+    """The reference CPU fitter compiled from its own sources (FP32 and the
+    float-promoted FP64 build). Present only where the reference sources are."""
+
+    def __init__(self):
+        if not reference_available():
+            _build.build_reference()
+        self._libs = {np.float32: ctypes.CDLL(os.path.join(_build.REF_DIR, "libref_f32.so")),
+                      np.float64: ctypes.CDLL(os.path.join(_build.REF_DIR, "libref_f64.so"))}
+        self._libs[np.float32].ref_eval_bspline_f32.restype = ctypes.c_float
+        self._libs[np.float32].ref_eval_bspline_f32.argtypes = [ctypes.c_float, ctypes.c_int]
+
+    def lib(self, dt):
+        return self._libs[dt]
+
+    def fit(self, rois, fittype, iterations, coeff, init_p=None, coeff3=None, precision="f32"):
+        dt = np.float32 if precision == "f32" else np.float64
+        return self._call(f"ref_fit{fittype}_{precision}", dt, rois, fittype, iterations, coeff,
+                          init_p, coeff3, None)
+
+    def eval_bspline(self, x, deg):
+        return self._libs[np.float32].ref_eval_bspline_f32(x, deg)

@@ -1,0 +1,132 @@
+"""bsfit: GB300-native B-spline PSF MLE fitter (fit types 6, 7, 8).
+
+Python mirror of the reference's MATLAB call surface over the C ABI of
+libbsfit.so:
+
+    P, CRLB, LL = GPUmleFit_LM_multiD(imstack, fittype, iterations, coeff,
+                                      varmap, silent, initP, coeff3)
+
+``imstack`` is a float32 array of shape (N, s, s) (the C-order view of the
+MATLAB [s, s, N] stack) or (s, s); ``coeff`` is the C-order view of the MATLAB
+coefficient array (shape (..., Z, X, Y)). Outputs: P (N, NV + 1) with the
+iteration count last, CRLB (N, NV), LL (N,), all float32.
+"""
+import numpy as np
+
+from . import _native
+from ._native import BsfitError, check
+
+NUM_PARAMS = {6: 5, 7: 6, 8: 8}
+
+_fp = _native._fp
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _dims(a):
+    return (np.ctypeslib.ctypes.c_int64 * a.ndim)(*reversed(a.shape))
+
+
+def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, silent=1,
+                        initP=None, coeff3=None):
+    """Drop-in for the reference mex (fit types 6, 7, 8); raises BsfitError."""
+    lib = _native.lib()
+    im = _f32(imstack)
+    if im.ndim == 2:
+        im = im[None]
+    if im.ndim != 3:
+        raise ValueError("imstack must be (N, s, s) or (s, s)")
+    n, s2, s1 = im.shape
+    fittype = int(fittype)
+    nv = NUM_PARAMS.get(fittype, 0)
+    c = _f32(coeff) if coeff is not None else None
+    c3 = _f32(coeff3) if coeff3 is not None else None
+    ip = _f32(np.atleast_1d(initP)) if initP is not None else None
+    vm = _f32(np.atleast_1d(varmap)) if varmap is not None else None
+    P = np.zeros((max(nv, 1) + 1, n), np.float32)
+    C = np.zeros((max(nv, 1), n), np.float32)
+    L = np.zeros(n, np.float32)
+    ptr = lambda a: a.ctypes.data_as(_fp) if a is not None else None  # noqa: E731
+    st = lib.bsfit_GPUmleFit_LM_multiD(
+        ptr(im), s1, s2, n, fittype, int(iterations),
+        ptr(c), c.ndim if c is not None else 0, _dims(c) if c is not None else None,
+        ptr(vm), vm.size if vm is not None else 0, int(silent),
+        ptr(ip), ip.size if ip is not None else 0,
+        ptr(c3), c3.ndim if c3 is not None else 0, _dims(c3) if c3 is not None else None,
+        ptr(P), ptr(C), ptr(L))
+    check(st, "GPUmleFit_LM_multiD")
+    return P.T.copy(), C.T.copy(), L
+
+
+class Model:
+    """A PSF model whose coefficient tables stay resident on the device."""
+
+    def __init__(self, fittype, coeff, coeff3=None, init_p=None):
+        lib = _native.lib()
+        self.fittype = int(fittype)
+        self.nv = NUM_PARAMS[self.fittype]
+        c = _f32(coeff)
+        c3 = _f32(coeff3) if coeff3 is not None else None
+        ip = _f32(np.atleast_1d(init_p)) if init_p is not None else None
+        h = np.ctypeslib.ctypes.c_void_p()
+        st = lib.bsfit_model_create(
+            self.fittype, c.ctypes.data_as(_fp), c.ndim, _dims(c),
+            c3.ctypes.data_as(_fp) if c3 is not None else None, c3.ndim if c3 is not None else 0,
+            _dims(c3) if c3 is not None else None,
+            ip.ctypes.data_as(_fp) if ip is not None else None, ip.size if ip is not None else 0,
+            np.ctypeslib.ctypes.byref(h))
+        check(st, "bsfit_model_create")
+        self._h = h
+
+    def fit_device(self, d_rois, roi_size, nfits, iterations, d_P, d_CRLB, d_LL, stream=0):
+        """Asynchronous fit with raw device pointers (ints) on a CUDA stream."""
+        st = _native.lib().bsfit_fit_device(self._h, d_rois, roi_size, nfits, iterations,
+                                            d_P, d_CRLB, d_LL, stream)
+        check(st, "bsfit_fit_device")
+
+    def fit_torch(self, rois, iterations, out=None, stream=None):
+        """Fit a CUDA float32 tensor (N, s, s); returns (P, CRLB, LL) tensors in
+        the reference's column-major layout: P (NV+1, N), CRLB (NV, N), LL (N)."""
+        import torch
+        assert rois.is_cuda and rois.dtype == torch.float32 and rois.is_contiguous()
+        n, s = rois.shape[0], rois.shape[-1]
+        if out is None:
+            P = torch.empty((self.nv + 1, n), device=rois.device, dtype=torch.float32)
+            C = torch.empty((self.nv, n), device=rois.device, dtype=torch.float32)
+            L = torch.empty((n,), device=rois.device, dtype=torch.float32)
+        else:
+            P, C, L = out
+        st = stream if stream is not None else torch.cuda.current_stream(rois.device)
+        self.fit_device(rois.data_ptr(), s, n, int(iterations), P.data_ptr(), C.data_ptr(),
+                        L.data_ptr(), st.cuda_stream)
+        return P, C, L
+
+    def eval_torch(self, rois, theta, fisher=False, stream=None):
+        """One evaluation per ROI at theta (tensor (NV, N)); returns (N, 1+NV+NH)."""
+        import torch
+        n, s = rois.shape[0], rois.shape[-1]
+        nh = self.nv * (self.nv + 1) // 2
+        out = torch.empty((n, 1 + self.nv + nh), device=rois.device, dtype=torch.float32)
+        theta = theta.contiguous()
+        st = stream if stream is not None else torch.cuda.current_stream(rois.device)
+        check(_native.lib().bsfit_eval_device(self._h, rois.data_ptr(), s, n, theta.data_ptr(),
+                                              int(bool(fisher)), out.data_ptr(), st.cuda_stream),
+              "bsfit_eval_device")
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.lib().bsfit_model_release(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def version():
+    return _native.lib().bsfit_version().decode()

@@ -1,0 +1,60 @@
+"""ctypes binding of libbsfit.so (the C ABI in include/bsfit.h).
+
+The library is required: importing this module on a machine where it has not
+been built raises, so there is no silent CPU fallback anywhere."""
+import ctypes
+import os
+
+from .build import LIB
+
+_lib = None
+
+_fp = ctypes.POINTER(ctypes.c_float)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+# name -> (restype, argtypes); mirrors include/bsfit.h
+SIGNATURES = {
+    "bsfit_status_str": (ctypes.c_char_p, [ctypes.c_int]),
+    "bsfit_version": (ctypes.c_char_p, []),
+    "bsfit_num_params": (ctypes.c_int, [ctypes.c_int32]),
+    "bsfit_GPUmleFit_LM_multiD": (ctypes.c_int, [
+        _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+        _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int64,
+        _fp, ctypes.c_int32, _i64p, _fp, _fp, _fp]),
+    "bsfit_model_create": (ctypes.c_int, [
+        ctypes.c_int32, _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int32, _i64p, _fp,
+        ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "bsfit_model_release": (ctypes.c_int, [ctypes.c_void_p]),
+    "bsfit_eval_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+        ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
+    "bsfit_fit_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise ImportError(f"{LIB} is not built: run __graft_entry__.build() first")
+        handle = ctypes.CDLL(LIB)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+class BsfitError(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = status
+        msg = lib().bsfit_status_str(status).decode()
+        super().__init__(f"{where}: bsfit status {status}: {msg}" if where else msg)
+
+
+def check(status, where=""):
+    if status != 0:
+        raise BsfitError(status, where)

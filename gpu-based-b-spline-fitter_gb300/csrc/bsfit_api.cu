@@ -1,0 +1,268 @@
+// Host library behind the C ABI declared in include/bsfit.h.
+//
+// It replaces the reference's mex boundary for the B-spline fit types
+// (VC/GPUmleFit_LM/mexFunction.cpp:208-762, VC = "MultiD_bspline/visual code"):
+// the same argument checks and error classes, returned as status codes; no
+// device is ever reset. Device buffers of the plain call come from the
+// stream-ordered allocator, so repeated calls reuse pooled memory instead of
+// allocating and freeing per call as the reference does.
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "../../include/bsfit.h"
+#include "bsfit_internal.h"
+
+using bsfit::FitArgs;
+using bsfit::ModelDev;
+
+struct bsfit_model_s {
+  ModelDev dev;
+  float* d_coeff = nullptr;
+  float* d_coeff3 = nullptr;
+};
+
+namespace {
+
+constexpr int kMaxRoi = 51;  // IMSZBIG (VC/GPUmleFit_LM/definitions.h:13)
+
+int num_params(int fittype) {
+  switch (fittype) {
+    case 6: return 5;
+    case 7: return 6;
+    case 8: return 8;
+    default: return 0;
+  }
+}
+
+int coeff_rank(int fittype) { return fittype == 6 ? 3 : fittype == 7 ? 4 : 5; }
+
+int check_coeff(int fittype, int ndim, const int64_t* dims) {
+  if (!dims) return BSFIT_E_WRONG_DATA_TYPE;
+  if (ndim != coeff_rank(fittype)) return BSFIT_E_COEFF_SIZE;
+  for (int i = 0; i < ndim; ++i)
+    if (dims[i] < 5 || dims[i] > (1 << 20)) return BSFIT_E_COEFF_SIZE;
+  // The reference indexes X rows with size(coeff, 1) and clamps Y with
+  // size(coeff, 2); unequal lateral sizes read outside the array there.
+  if (dims[0] != dims[1]) return BSFIT_E_COEFF_SIZE;
+  return BSFIT_OK;
+}
+
+void fill_model(ModelDev& m, int fittype, const int64_t* dims, const float* init_p,
+                int64_t init_p_numel) {
+  std::memset(&m, 0, sizeof(m));
+  m.fittype = fittype;
+  int r = coeff_rank(fittype);
+  int64_t st = 1;
+  for (int i = 0; i < 5; ++i) {
+    m.cd[i] = i < r ? (int)dims[i] : 1;
+    m.st[i] = st;
+    st *= m.cd[i];
+  }
+  m.n[0] = m.cd[1] - 3;
+  m.n[1] = m.cd[0] - 3;
+  for (int i = 2; i < r; ++i) m.n[i] = m.cd[i] - 3;
+  m.init_p_len = 0;
+  if (init_p) {
+    int k = (int)(init_p_numel < 4 ? init_p_numel : 4);
+    for (int i = 0; i < k; ++i) m.init_p[i] = init_p[i];
+    m.init_p_len = k;
+  }
+}
+
+int64_t numel(int ndim, const int64_t* dims) {
+  int64_t n = 1;
+  for (int i = 0; i < ndim; ++i) n *= dims[i];
+  return n;
+}
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return BSFIT_OK;
+  if (e == cudaErrorMemoryAllocation) return BSFIT_E_NOT_ENOUGH_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return BSFIT_E_NO_DEVICE;
+  return BSFIT_E_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bsfit_status_str(int status) {
+  switch (status) {
+    case BSFIT_OK: return "ok";
+    case BSFIT_E_WRONG_NO_ARGS:
+      return "Inputs must include: GPUmleFit_LM(data,fittype,iterations,startparameter,var,silent)";
+    case BSFIT_E_WRONG_DATA_TYPE: return "Data must be comprised of single floats (missing array)";
+    case BSFIT_E_SUBREGION_SIZE: return "X,Y dimension of data must be smaller than 51";
+    case BSFIT_E_SUBREGION_SHAPE: return "Fit Box must be square";
+    case BSFIT_E_UNSUPPORTED_FITTYPE: return "fit type not supported (B-spline fit types are 6, 7, 8)";
+    case BSFIT_E_NOT_ENOUGH_MEMORY: return "Not enough memory on the GPU";
+    case BSFIT_E_CUDA: return "CUDA call failed";
+    case BSFIT_E_NO_DEVICE: return "No CUDA capable devices were detected";
+    case BSFIT_E_COEFF_SIZE: return "coefficient array has the wrong rank or size";
+    case BSFIT_E_INIT_P: return "initP missing or too short for this fit type";
+    case BSFIT_E_INVALID: return "invalid argument";
+    case BSFIT_E_TIMEOUT: return "bounded device wait timed out";
+    default: return "unknown status";
+  }
+}
+
+const char* bsfit_version(void) { return "bsfit-gb300 0.1 (sm_103a)"; }
+
+int bsfit_num_params(int32_t fittype) { return num_params(fittype); }
+
+int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
+                       const int64_t* coeff_dims, const float* coeff3, int32_t coeff3_ndim,
+                       const int64_t* coeff3_dims, const float* init_p, int64_t init_p_numel,
+                       bsfit_model* out) {
+  if (!out) return BSFIT_E_INVALID;
+  *out = nullptr;
+  if (num_params(fittype) == 0) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (!coeff) return BSFIT_E_WRONG_DATA_TYPE;
+  int st = check_coeff(fittype, coeff_ndim, coeff_dims);
+  if (st) return st;
+  if (fittype == 7 && (!init_p || init_p_numel < 2)) return BSFIT_E_INIT_P;
+  if (fittype == 8) {
+    if (init_p && init_p_numel < 4) return BSFIT_E_INIT_P;
+    if (!coeff3 || !coeff3_dims || coeff3_ndim != 3) return BSFIT_E_WRONG_DATA_TYPE;
+    for (int i = 0; i < 3; ++i)
+      if (coeff3_dims[i] != coeff_dims[i]) return BSFIT_E_COEFF_SIZE;
+  }
+  if (fittype == 8) return BSFIT_E_UNSUPPORTED_FITTYPE;  // kernel not built yet
+  bsfit_model_s* m = new (std::nothrow) bsfit_model_s;
+  if (!m) return BSFIT_E_NOT_ENOUGH_MEMORY;
+  fill_model(m->dev, fittype, coeff_dims, init_p, init_p_numel);
+  size_t bytes = (size_t)numel(coeff_ndim, coeff_dims) * sizeof(float);
+  cudaError_t e = cudaMalloc(&m->d_coeff, bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_coeff, coeff, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && fittype == 8) {
+    size_t b3 = (size_t)numel(3, coeff3_dims) * sizeof(float);
+    e = cudaMalloc(&m->d_coeff3, b3);
+    if (e == cudaSuccess) e = cudaMemcpy(m->d_coeff3, coeff3, b3, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    cudaFree(m->d_coeff);
+    cudaFree(m->d_coeff3);
+    delete m;
+    return cuda_status(e);
+  }
+  m->dev.coeff = m->d_coeff;
+  m->dev.coeff3 = m->d_coeff3;
+  *out = m;
+  return BSFIT_OK;
+}
+
+int bsfit_model_release(bsfit_model model) {
+  if (!model) return BSFIT_E_INVALID;
+  cudaFree(model->d_coeff);
+  cudaFree(model->d_coeff3);
+  delete model;
+  return BSFIT_OK;
+}
+
+int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                     int32_t iterations, float* d_P, float* d_CRLB, float* d_LL, void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  FitArgs a;
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  a.out_n = nfits;
+  a.out_offset = 0;
+  return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
+}
+
+int bsfit_eval_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                      const float* d_theta, int32_t fisher, float* d_out, void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_theta || !d_out) return BSFIT_E_INVALID;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  return cuda_status(bsfit::launch_eval(a, d_theta, d_out, fisher, (cudaStream_t)stream));
+}
+
+int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                              int64_t nfits, int32_t fittype, int32_t iterations,
+                              const float* coeff, int32_t coeff_ndim, const int64_t* coeff_dims,
+                              const float* varmap, int64_t varmap_numel, int32_t silent,
+                              const float* init_p, int64_t init_p_numel, const float* coeff3,
+                              int32_t coeff3_ndim, const int64_t* coeff3_dims, float* P,
+                              float* CRLB, float* LL) {
+  (void)varmap;
+  (void)varmap_numel;  // ignored for fit types 6-8, as in the reference
+  // Argument checks in the reference's order (mex :247-263).
+  if (!imstack) return BSFIT_E_WRONG_DATA_TYPE;
+  if (roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (roi_size2 != roi_size) return BSFIT_E_SUBREGION_SHAPE;
+  if (roi_size < 1 || nfits < 0) return BSFIT_E_INVALID;
+  if (num_params(fittype) == 0) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (!P || !CRLB || !LL) return BSFIT_E_INVALID;
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count < 1) return BSFIT_E_NO_DEVICE;
+  const int nv = num_params(fittype);
+  if (!silent) {
+    std::printf("subregion size: %lld fittype: %d\n", (long long)roi_size, fittype);
+    std::printf("Number of fits: %lld no padding\n", (long long)nfits);
+  }
+  bsfit_model model = nullptr;
+  int st = bsfit_model_create(fittype, coeff, coeff_ndim, coeff_dims, coeff3, coeff3_ndim,
+                              coeff3_dims, init_p, init_p_numel, &model);
+  if (st) return st;
+  if (nfits == 0) {
+    bsfit_model_release(model);
+    return BSFIT_OK;
+  }
+  // Memory check (mex :409-456): refuse work above 95% of free memory.
+  const size_t s2 = (size_t)roi_size * roi_size;
+  const size_t in_bytes = (size_t)nfits * s2 * sizeof(float);
+  const size_t out_bytes = (size_t)nfits * (2 * nv + 2) * sizeof(float);
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+      (double)(in_bytes + out_bytes) > 0.95 * (double)free_b) {
+    bsfit_model_release(model);
+    return BSFIT_E_NOT_ENOUGH_MEMORY;
+  }
+  cudaStream_t stream = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  float *d_rois = nullptr, *d_out = nullptr;
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_rois, in_bytes, stream);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_out, out_bytes, stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rois, imstack, in_bytes, cudaMemcpyHostToDevice, stream);
+  float* d_P = d_out;
+  float* d_C = d_P + (size_t)nfits * (nv + 1);
+  float* d_L = d_C + (size_t)nfits * nv;
+  if (e == cudaSuccess) {
+    st = bsfit_fit_device(model, d_rois, roi_size, nfits, iterations, d_P, d_C, d_L, stream);
+    if (st) e = cudaErrorUnknown;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(P, d_P, (size_t)nfits * (nv + 1) * sizeof(float), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(CRLB, d_C, (size_t)nfits * nv * sizeof(float), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(LL, d_L, (size_t)nfits * sizeof(float), cudaMemcpyDeviceToHost, stream);
+  if (d_rois) cudaFreeAsync(d_rois, stream);
+  if (d_out) cudaFreeAsync(d_out, stream);
+  cudaError_t e2 = stream ? cudaStreamSynchronize(stream) : cudaSuccess;
+  if (stream) cudaStreamDestroy(stream);
+  bsfit_model_release(model);
+  if (st) return st;
+  if (e == cudaSuccess) e = e2;
+  return cuda_status(e);
+}
+
+}  // extern "C"

@@ -1,0 +1,744 @@
+// Per-ROI Levenberg-Marquardt Poisson-MLE fit of a cubic B-spline PSF,
+// one warp per ROI, for fit types 6 (3D), 7 (4D colour) and 8 (5D + 3D).
+//
+// Method: the reference CPU fitter, VC/CPUmleFit_LM/CPUmleFit_LM.cpp:2411-3620
+// (VC = "MultiD_bspline/visual code"), with the same initial guesses, damping
+// schedule, clamps, bounds, quirks and iteration cap. The arithmetic is
+// reorganised for the GPU:
+//
+//  * Model evaluation is separable. For one ROI evaluation all pixels share the
+//    non-lateral knot (z, w, u) and the fractional positions, and pixel (ii, jj)
+//    only moves the lateral knots. The warp therefore (A) contracts the
+//    non-lateral axes at every lateral node of the ROI's knot window into
+//    shared-memory maps (value and one map per non-lateral derivative), (B)
+//    contracts the Y axis for every (X node, pixel row), and (C) contracts the
+//    X axis per pixel, fused with the Poisson deviance, gradient and Hessian.
+//    This is the tensor-product sum of CPUsplineLib.cpp:1199-1288 (3D),
+//    :761-970 (4D), :43-475 (5D) in a different summation order.
+//  * Derivatives keep the reference's "difference of neighbouring
+//    coefficients times the quadratic basis" form along every axis.
+//  * Reductions are warp butterflies; the deviance is accumulated as a
+//    compensated FP32 pair, since it drives the convergence test.
+//  * The LM step is an FP32 Cholesky solve (CPUsplineLib.cpp:1363-1419) plus
+//    one refinement step whose residual is computed with error-free FP32
+//    products (float-float), instead of FP64: GB300 issues FP64 at 1/57 of the
+//    FP32 rate and a one-lane FP64 instruction costs as much as a full warp.
+//  * The Fisher information is inverted in FP64 once per fit with the
+//    reference's unpivoted LU (VC/CPUmleFit_LM/MatInvLib.h:17-77).
+//
+// Every global read of the coefficient arrays stays inside the array: the
+// knots are clamped exactly as in the reference, and the one coefficient the
+// reference reads past its knot window (the zero-weight fifth node of a
+// derivative difference) is never read.
+#include <cstdint>
+#include <cstdio>
+
+#include "bsfit_device.cuh"
+#include "bsfit_internal.h"
+
+namespace bsfit {
+
+template <int MODE>
+struct ModeTraits;
+
+template <>
+struct ModeTraits<6> {
+  static constexpr int D = 3;   // spline dimensions
+  static constexpr int NV = 5;  // fitted parameters
+  static constexpr int NA = 2;  // non-lateral maps: value, d/dz
+  static constexpr int NG = 3;  // after the Y pass: value, d/dY, d/dz
+};
+template <>
+struct ModeTraits<7> {
+  static constexpr int D = 4;
+  static constexpr int NV = 6;
+  static constexpr int NA = 3;  // value, d/dz, d/dw
+  static constexpr int NG = 4;  // value, d/dY, d/dz, d/dw
+};
+
+// Per-warp shared-memory layout (floats). WP = s + 4 bounds the knot window
+// along each lateral axis.
+struct WarpLayout {
+  int s, s2p, wp, na, ng;
+  __host__ __device__ int off_kx() const { return s2p; }
+  __host__ __device__ int off_ky() const { return s2p + ((s + 3) & ~3); }
+  __host__ __device__ int off_w() const { return off_ky() + ((s + 3) & ~3); }
+  __host__ __device__ int off_a() const { return off_w() + 40; }
+  __host__ __device__ int off_g() const { return off_a() + na * wp * wp; }
+  __host__ __device__ int total() const { return off_g() + ng * wp * s; }
+};
+
+__host__ __device__ inline WarpLayout make_layout(int mode, int s) {
+  WarpLayout L;
+  L.s = s;
+  L.s2p = (s * s + 3) & ~3;
+  L.wp = s + 4;
+  L.na = mode == 6 ? 2 : 3;
+  L.ng = mode == 6 ? 3 : 4;
+  return L;
+}
+
+int warp_smem_floats(int mode, int s) { return make_layout(mode, s).total(); }
+
+// ---------------------------------------------------------------------------
+// One ROI evaluation: deviance, gradient and Hessian (or Fisher information and
+// log-likelihood when FISHER is set) at theta.
+
+template <int MODE>
+struct Eval {
+  using T = ModeTraits<MODE>;
+  static constexpr int D = T::D;
+  static constexpr int NV = T::NV;
+  static constexpr int NH = NV * (NV + 1) / 2;
+};
+
+template <int MODE, bool FISHER>
+__device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int lane,
+                         const float* th, bool dup45, FPair& err_out, float (&jac)[ModeTraits<MODE>::NV],
+                         float (&hes)[ModeTraits<MODE>::NV * (ModeTraits<MODE>::NV + 1) / 2]) {
+  using TR = ModeTraits<MODE>;
+  constexpr int D = TR::D;
+  constexpr int NV = TR::NV;
+  constexpr int NH = NV * (NV + 1) / 2;
+  const int s = L.s;
+  const ModelDev& m = a.m;
+  float* data = ws;
+  int* kxs = reinterpret_cast<int*>(ws + L.off_kx());
+  int* kys = reinterpret_cast<int*>(ws + L.off_ky());
+  float* w = ws + L.off_w();
+  float* A = ws + L.off_a();
+  float* G = ws + L.off_g();
+  const int wp = L.wp;
+  __syncwarp();  // the previous evaluation's readers of kxs / w / G are done
+
+  // Positions (CPUmleFit_LM.cpp:2512-2523): pixel jj sits at
+  // (xc + jj) + off along X, pixel ii at (yc + ii) + off along Y.
+  const float xc = (float)((s + 1) / 2) - th[0];
+  const float yc = (float)((s + 1) / 2) - th[1];
+  const float off = (float)(m.n[1] - s) / 2.0f;
+  const float zc = th[4];
+  const float wc = (D >= 4) ? th[5] : 0.0f;
+
+  for (int j = lane; j < s; j += 32) {
+    kxs[j] = knot_index((xc + (float)j) + off, m.n[1]);
+    kys[j] = knot_index((yc + (float)j) + off, m.n[0]);
+  }
+  // Fractional parts (Y, X, Z, W) and the 1-D weights, one per lane.
+  {
+    float fr[4];
+    fr[0] = yc - floorf(yc);
+    fr[1] = xc - floorf(xc);
+    fr[2] = zc - floorf(zc);
+    fr[3] = wc - floorf(wc);
+    if (lane < 7 * D) {
+      int ax = lane / 7;
+      w[ax * 8 + (lane % 7)] = axis_weight(fr[ax], lane % 7);
+    }
+  }
+  __syncwarp();
+  int kxmin, kxmax, kymin, kymax;
+  {
+    int a0 = INT_MAX, a1 = INT_MIN, b0 = INT_MAX, b1 = INT_MIN;
+    for (int j = lane; j < s; j += 32) {
+      a0 = min(a0, kxs[j]);
+      a1 = max(a1, kxs[j]);
+      b0 = min(b0, kys[j]);
+      b1 = max(b1, kys[j]);
+    }
+    kxmin = warp_min(a0);
+    kxmax = warp_max(a1);
+    kymin = warp_min(b0);
+    kymax = warp_max(b1);
+  }
+  // Window of lateral nodes [k - 1, k + 2] over all pixels. Its extent is at
+  // most s + 4 (the per-pixel knots grow by one per pixel, plus one for
+  // rounding); the caps keep every shared-memory access inside the warp's maps.
+  const int xb = kxmin - 1, wx = min(kxmax - kxmin + 4, wp);
+  const int yb = kymin - 1, wy = min(kymax - kymin + 4, wp);
+  const int kz = knot_index(zc, m.n[2]);
+  const int kw = (D >= 4) ? knot_index(wc, m.n[3]) : 0;
+
+  // (A) Non-lateral contraction at every lateral node of the window.
+  {
+    const float* wz = w + 2 * 8;
+    const float bz0 = wz[0], bz1 = wz[1], bz2 = wz[2], bz3 = wz[3];
+    const float dz0 = wz[4], dz1 = wz[5], dz2 = wz[6];
+    const int64_t sz_ = m.st[2];
+    const int nodes = wx * wy;
+    if constexpr (D == 3) {
+      const float* base = m.coeff + (int64_t)(kz - 1) * sz_;
+      for (int t = lane; t < nodes; t += 32) {
+        int xr = t / wy, yr = t - xr * wy;
+        const float* p = base + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
+        float c0 = __ldg(p), c1 = __ldg(p + sz_), c2 = __ldg(p + 2 * sz_), c3 = __ldg(p + 3 * sz_);
+        float v = c0 * bz0 + c1 * bz1 + c2 * bz2 + c3 * bz3;
+        float dz = (c1 - c0) * dz0 + (c2 - c1) * dz1 + (c3 - c2) * dz2;
+        A[xr * wp + yr] = v;
+        A[wp * wp + xr * wp + yr] = dz;
+      }
+    } else {
+      const float* ww = w + 3 * 8;
+      const float bw[4] = {ww[0], ww[1], ww[2], ww[3]};
+      const float dw[3] = {ww[4], ww[5], ww[6]};
+      const int64_t sw_ = m.st[3];
+      const float* base = m.coeff + (int64_t)(kz - 1) * sz_ + (int64_t)(kw - 1) * sw_;
+      for (int t = lane; t < nodes; t += 32) {
+        int xr = t / wy, yr = t - xr * wy;
+        const float* p = base + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
+        float vz[4], dzv[4];
+#pragma unroll
+        for (int iw = 0; iw < 4; ++iw) {
+          const float* q = p + iw * sw_;
+          float c0 = __ldg(q), c1 = __ldg(q + sz_), c2 = __ldg(q + 2 * sz_), c3 = __ldg(q + 3 * sz_);
+          vz[iw] = c0 * bz0 + c1 * bz1 + c2 * bz2 + c3 * bz3;
+          dzv[iw] = (c1 - c0) * dz0 + (c2 - c1) * dz1 + (c3 - c2) * dz2;
+        }
+        float v = vz[0] * bw[0] + vz[1] * bw[1] + vz[2] * bw[2] + vz[3] * bw[3];
+        float dz = dzv[0] * bw[0] + dzv[1] * bw[1] + dzv[2] * bw[2] + dzv[3] * bw[3];
+        float dwv = (vz[1] - vz[0]) * dw[0] + (vz[2] - vz[1]) * dw[1] + (vz[3] - vz[2]) * dw[2];
+        A[xr * wp + yr] = v;
+        A[wp * wp + xr * wp + yr] = dz;
+        A[2 * wp * wp + xr * wp + yr] = dwv;
+      }
+    }
+  }
+  __syncwarp();
+
+  // (B) Y contraction for every (X node, pixel row ii).
+  {
+    const float by0 = w[0], by1 = w[1], by2 = w[2], by3 = w[3];
+    const float dy0 = w[4], dy1 = w[5], dy2 = w[6];
+    const int items = wx * s;
+    const int gstride = wp * s;
+    for (int t = lane; t < items; t += 32) {
+      int xr = t / s, py = t - xr * s;
+      int oy = min(max(kys[py] - 1 - yb, 0), wy - 4);
+      const float* a0 = A + xr * wp + oy;
+      float v0 = a0[0], v1 = a0[1], v2 = a0[2], v3 = a0[3];
+      G[xr * s + py] = v0 * by0 + v1 * by1 + v2 * by2 + v3 * by3;
+      G[gstride + xr * s + py] = (v1 - v0) * dy0 + (v2 - v1) * dy1 + (v3 - v2) * dy2;
+#pragma unroll
+      for (int c = 1; c < TR::NA; ++c) {
+        const float* ac = a0 + c * wp * wp;
+        G[(c + 1) * gstride + xr * s + py] = ac[0] * by0 + ac[1] * by1 + ac[2] * by2 + ac[3] * by3;
+      }
+    }
+  }
+  __syncwarp();
+
+  // (C) X contraction per pixel, fused with the likelihood sums.
+  FPair err{0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < NV; ++k) jac[k] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < NH; ++k) hes[k] = 0.0f;
+  {
+    const float bx0 = w[8], bx1 = w[9], bx2 = w[10], bx3 = w[11];
+    const float dx0 = w[12], dx1 = w[13], dx2 = w[14];
+    const float N = th[2], bg = th[3];
+    const int gstride = wp * s;
+    const int s2 = s * s;
+    for (int p = lane; p < s2; p += 32) {
+      int px = p / s, py = p - px * s;  // px = jj (X), py = ii (Y)
+      int ox = min(max(kxs[px] - 1 - xb, 0), wx - 4);
+      const float* g = G + ox * s + py;
+      float g0 = g[0], g1 = g[s], g2 = g[2 * s], g3 = g[3 * s];
+      float f = g0 * bx0 + g1 * bx1 + g2 * bx2 + g3 * bx3;
+      float dX = (g1 - g0) * dx0 + (g2 - g1) * dx1 + (g3 - g2) * dx2;
+      const float* gy = g + gstride;
+      float dY = gy[0] * bx0 + gy[s] * bx1 + gy[2 * s] * bx2 + gy[3 * s] * bx3;
+      float dudt[NV];
+      dudt[0] = -N * dX;
+      dudt[1] = -N * dY;
+      dudt[2] = f;
+      dudt[3] = 1.0f;
+#pragma unroll
+      for (int c = 1; c < TR::NA; ++c) {
+        const float* gc = g + (c + 1) * gstride;
+        float dc = gc[0] * bx0 + gc[s] * bx1 + gc[2 * s] * bx2 + gc[3 * s] * bx3;
+        dudt[3 + c] = N * dc;
+      }
+      if (MODE == 7 && dup45) dudt[5] = dudt[4];
+      const float model = bg + N * f;
+      float d = data[p];
+      if (!FISHER) {
+        // CPUmleFit_LM.cpp:2540-2559
+        float term;
+        if (d > 0.0f) {
+          term = 2.0f * ((model - d) - d * logf(model / d));
+        } else {
+          term = 2.0f * model;
+          d = 0.0f;
+        }
+        err.add(term);
+        const float t1 = 1.0f - d / model;
+        const float t2 = d / (model * model);
+#pragma unroll
+        for (int l = 0; l < NV; ++l) jac[l] = fmaf(t1, dudt[l], jac[l]);
+        int k = 0;
+#pragma unroll
+        for (int l = 0; l < NV; ++l) {
+          const float tl = t2 * dudt[l];
+#pragma unroll
+          for (int mm = l; mm < NV; ++mm, ++k) hes[k] = fmaf(tl, dudt[mm], hes[k]);
+        }
+      } else {
+        // Fisher information and log-likelihood (CPUmleFit_LM.cpp:2730-2742).
+        const float im = 1.0f / model;
+        int k = 0;
+#pragma unroll
+        for (int l = 0; l < NV; ++l) {
+          const float tl = dudt[l] * im;
+#pragma unroll
+          for (int mm = l; mm < NV; ++mm, ++k) hes[k] = fmaf(tl, dudt[mm], hes[k]);
+        }
+        if (model > 0.0f) {
+          float ll = (d > 0.0f) ? (d * logf(model) - model - d * logf(d) + d) : -model;
+          err.add(ll);
+        }
+      }
+    }
+  }
+  warp_sum_array<NV>(jac);
+  warp_sum_array<NH>(hes);
+  err_out = warp_sum_pair(err);
+}
+
+// ---------------------------------------------------------------------------
+// LM helpers (warp-uniform register state).
+
+template <int NV>
+__device__ __forceinline__ int hidx(int l, int m) {
+  // index of (l, m), l <= m, in the packed upper triangle
+  return l * NV - (l * (l - 1)) / 2 + (m - l);
+}
+
+// Unpivoted Cholesky of the full matrix a (row-major NV x NV), lower factor in
+// u (u[i*NV + j], j <= i). Fails on a negative pivot only
+// (CPUsplineLib.cpp:1363-1390).
+template <int NV>
+__device__ __forceinline__ bool cholesky(const float (&a)[NV * NV], float (&u)[NV * NV]) {
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+#pragma unroll
+    for (int j = 0; j <= i; j++) {
+      float s = 0.0f;
+#pragma unroll
+      for (int k = 0; k < j; k++) s = fmaf(u[i * NV + k], u[j * NV + k], s);
+      if (i == j) {
+        float piv = a[i * NV + i] - s;
+        if (!(piv >= 0.0f)) return false;
+        u[i * NV + j] = sqrtf(piv);
+      } else {
+        u[i * NV + j] = (a[i * NV + j] - s) / u[j * NV + j];
+      }
+    }
+  }
+  return true;
+}
+
+template <int NV>
+__device__ __forceinline__ void chol_solve(const float (&u)[NV * NV], const float (&b)[NV],
+                                           float (&x)[NV]) {
+  float y[NV];
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    float t = b[i];
+#pragma unroll
+    for (int j = 0; j < i; j++) t -= u[i * NV + j] * y[j];
+    y[i] = t / u[i * NV + i];
+  }
+#pragma unroll
+  for (int i = NV - 1; i >= 0; i--) {
+    float t = y[i];
+#pragma unroll
+    for (int j = i + 1; j < NV; j++) t -= u[j * NV + i] * x[j];
+    x[i] = t / u[i * NV + i];
+  }
+}
+
+// Unpivoted LU inverse diagonal in FP64 (VC/CPUmleFit_LM/MatInvLib.h:17-77).
+// A parameter whose model derivative is exactly zero at every pixel (z on the
+// mirror-padded boundary knot, for instance) has an exactly zero Fisher row and
+// column. The reference's FP64 arithmetic turns that into a huge finite
+// variance from rounding noise; here the row is decoupled explicitly: its
+// diagonal is set to the smallest positive double, so its variance overflows
+// to +inf in FP32 and the other parameters' variances are unaffected.
+template <int NV>
+__device__ void mat_inv_diag(double (&M)[NV * NV], double (&diag)[NV]) {
+  for (int i = 0; i < NV; i++)
+    if (M[i * NV + i] == 0.0) M[i * NV + i] = 4.9406564584124654e-324;
+  double Minv[NV * NV];
+  for (int jj = 0; jj < NV; jj++) {
+    for (int ii = 1; ii <= jj; ii++) {
+      double t = 0.0;
+      for (int kk = 0; kk <= ii - 1; kk++) t += M[ii + kk * NV] * M[kk + jj * NV];
+      M[ii + jj * NV] -= t;
+    }
+    for (int ii = jj + 1; ii < NV; ii++) {
+      double t = 0.0;
+      for (int kk = 0; kk <= jj - 1; kk++) t += M[ii + kk * NV] * M[kk + jj * NV];
+      M[ii + jj * NV] = (1.0 / M[jj + jj * NV]) * (M[ii + jj * NV] - t);
+    }
+  }
+  for (int num = 0; num < NV; num++) {
+    double yy[NV];
+    yy[0] = (num == 0) ? 1.0 : 0.0;
+    for (int ii = 1; ii < NV; ii++) {
+      double t = 0.0;
+      for (int jj = 0; jj <= ii - 1; jj++) t += M[ii + jj * NV] * yy[jj];
+      yy[ii] = ((ii == num) ? 1.0 : 0.0) - t;
+    }
+    Minv[NV - 1 + num * NV] = yy[NV - 1] / M[(NV - 1) + (NV - 1) * NV];
+    for (int ii = NV - 2; ii >= 0; ii--) {
+      double t = 0.0;
+      for (int jj = ii + 1; jj < NV; jj++) t += M[ii + jj * NV] * Minv[jj + num * NV];
+      Minv[ii + num * NV] = (1.0 / M[ii + ii * NV]) * (yy[ii] - t);
+    }
+  }
+  for (int i = 0; i < NV; i++) diag[i] = Minv[i * NV + i];
+}
+
+// ---------------------------------------------------------------------------
+// One ROI, one warp.
+
+template <int MODE>
+__device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int lane, int64_t roi) {
+  using TR = ModeTraits<MODE>;
+  constexpr int NV = TR::NV;
+  constexpr int NH = NV * (NV + 1) / 2;
+  const int s = L.s;
+  const int s2 = s * s;
+  float* data = ws;
+  const float* src = a.rois + roi * (int64_t)s2;
+  for (int p = lane; p < s2; p += 32) data[p] = __ldg(src + p);
+  __syncwarp();
+
+  // Initial guesses (CPUgaussLib.cpp:172-225, CPUmleFit_LM.cpp:2477-2482).
+  float th[NV];
+  {
+    FPair tx{0.f, 0.f}, ty{0.f, 0.f}, ts{0.f, 0.f};
+    float mx = 0.0f, mn = 10e10f;
+    bool nan_seen = false;
+    for (int p = lane; p < s2; p += 32) {
+      float d = data[p];
+      int jj = p / s, ii = p - jj * s;
+      tx.add(d * (float)ii);
+      ty.add(d * (float)jj);
+      ts.add(d);
+      nan_seen |= (d != d);
+      mx = (mx > d) ? mx : d;
+      mn = (mn < d) ? mn : d;
+    }
+    tx = warp_sum_pair(tx);
+    ty = warp_sum_pair(ty);
+    ts = warp_sum_pair(ts);
+    float tsum = ts.hi + ts.lo;
+    th[0] = (tx.hi + tx.lo) / tsum;
+    th[1] = (ty.hi + ty.lo) / tsum;
+    if (__any_sync(kFull, nan_seen)) {
+      // The reference's max/min fold is order dependent with NaN pixels:
+      // replay it sequentially.
+      mx = 0.0f;
+      mn = 10e10f;
+      for (int p0 = 0; p0 < s2; ++p0) {
+        int kk = p0 / s, ll = p0 - kk * s;
+        float d = data[kk * s + ll];
+        mx = (mx > d) ? mx : d;
+        mn = (mn < d) ? mn : d;
+      }
+    } else {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+        mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
+      }
+    }
+    // N0 = max(0, (max - min) * 2 * pi * 1.5 * 1.5), bg0 = max(min, 0.01),
+    // evaluated in double as in the reference's expression.
+    double n0 = ((double)mx - (double)mn) * 2.0 * (double)3.141592f * 1.5 * 1.5;
+    th[2] = (float)((0.0 > n0) ? 0.0 : n0);
+    th[3] = (float)(((double)mn > 0.01) ? (double)mn : 0.01);
+    if (MODE == 6) {
+      th[4] = (float)a.m.n[2] / 2.0f;
+    } else if (MODE == 7) {
+      if (a.m.init_p_len >= 2 && a.m.init_p[0] != 0.0f) {
+        th[4] = a.m.init_p[0];
+        th[5] = a.m.init_p[1];
+      } else {
+        th[4] = (float)a.m.n[2] / 2.0f;
+        th[5] = (float)a.m.n[3] / 2.0f;
+      }
+    }
+  }
+
+  // LM state (CPUmleFit_LM.cpp:2425-2450).
+  float oth[NV], sign[NV], osign[NV], clampv[NV], oclamp[NV], fade[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    oth[i] = th[i];
+    sign[i] = 0.0f;
+    osign[i] = 0.0f;
+  }
+  if (MODE == 6) {
+    const float c[5] = {2.0f, 2.0f, 10000.0f, 20.0f, 20.0f};
+#pragma unroll
+    for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = c[i % 5], fade[i] = 0.5f;
+  } else {
+    const float c[6] = {1.0f, 1.0f, 10000.0f, 20.0f, 2.0f, 0.00001f};
+    const float fd[6] = {0.5f, 0.5f, 0.4f, 0.5f, 0.7f, 0.8f};
+#pragma unroll
+    for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = c[i % 6], fade[i] = fd[i % 6];
+  }
+  float lambda = 1.0f, olambda = 1.0f;
+  FPair err{1e12f, 0.0f}, oerr{1e13f, 0.0f};
+  float jac[NV], hes[NH];
+  int turn = 1;
+
+  evaluate<MODE, false>(a, L, ws, lane, th, MODE == 7, err, jac, hes);
+
+  int kk = 0;
+  for (kk = 0; kk < a.iterations; kk++) {
+    // |(newErr - oldErr) / newErr| < 1e-6 (CPUmleFit_LM.cpp:2565)
+    {
+      float dhi = err.hi - oerr.hi;
+      float dlo = err.lo - oerr.lo;
+      float rel = fabsf((dhi + dlo) / (err.hi + err.lo));
+      if (rel < 1e-6f) break;
+    }
+    const float e_new = err.hi + err.lo, e_old = oerr.hi + oerr.lo;
+    if ((double)e_new > 1.5 * (double)e_old) {
+#pragma unroll
+      for (int i = 0; i < NV; i++) {
+        sign[i] = osign[i];
+        clampv[i] = oclamp[i];
+        th[i] = oth[i];
+      }
+      lambda = olambda;
+      err = oerr;
+      lambda = 10.0f * lambda;
+    } else if (e_new < e_old) {
+      if (lambda > 1.0f)
+        lambda = (float)((double)lambda * 0.8);
+      else if (lambda < 1.0f)
+        lambda = 1.0f;
+    }
+    // H_ii *= lambda, in place (cumulative across failed solves, as in the
+    // reference).
+#pragma unroll
+    for (int i = 0; i < NV; i++) hes[hidx<NV>(i, i)] *= lambda;
+    float full[NV * NV], u[NV * NV], upd[NV];
+#pragma unroll
+    for (int l = 0; l < NV; ++l)
+#pragma unroll
+      for (int mm = l; mm < NV; ++mm) full[l * NV + mm] = full[mm * NV + l] = hes[hidx<NV>(l, mm)];
+    bool ok = cholesky<NV>(full, u);
+    if (ok) {
+      chol_solve<NV>(u, jac, upd);
+      // One refinement step: r = J - H upd with error-free products.
+      float r[NV];
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        float sh = jac[i], sl = 0.0f;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+          float p, pe, t, te;
+          two_prod(full[i * NV + j], upd[j], p, pe);
+          two_sum(sh, -p, t, te);
+          sh = t;
+          sl += te - pe;
+        }
+        r[i] = sh + sl;
+      }
+      float corr[NV];
+      chol_solve<NV>(u, r, corr);
+#pragma unroll
+      for (int i = 0; i < NV; ++i) upd[i] += corr[i];
+      if (MODE != 6) {
+        bool bad = false;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) bad |= (upd[i] != upd[i]);
+        if (bad) ok = false;  // CPUmleFit_LM.cpp:2943-2950
+      }
+    }
+    if (ok) {
+      if (MODE == 7) upd[5] = upd[5] * 10.0f;  // :2951
+#pragma unroll
+      for (int i = 0; i < NV; i++) {
+        osign[i] = sign[i];
+        oclamp[i] = clampv[i];
+        oth[i] = th[i];
+      }
+      olambda = lambda;
+      oerr = err;
+      if (MODE == 7) {
+        // "let it go" (:2966-2971)
+        if (fabsf(upd[4]) < 0.005f && turn) {
+          clampv[5] = (float)a.m.n[3] / 10.0f;
+          oclamp[5] = clampv[5];
+          turn = 0;
+          clampv[4] = 2.0f;
+          oclamp[4] = 2.0f;
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        if (sign[l] != 0.0f) {
+          if ((sign[l] == 1.0f && upd[l] < 0.0f) || (sign[l] == -1.0f && upd[l] > 0.0f))
+            clampv[l] = clampv[l] * fade[l];
+        }
+        sign[l] = (upd[l] > 0.0f) ? 1.0f : -1.0f;
+        th[l] = th[l] - upd[l] / (1.0f + fabsf(upd[l] / clampv[l]));
+      }
+      th[2] = (th[2] > 1.0f) ? th[2] : 1.0f;
+      th[3] = ((double)th[3] > 0.01) ? th[3] : 0.01f;
+      th[4] = (th[4] > 0.0f) ? th[4] : 0.0f;
+      if (MODE == 6) {
+        float zmax = (float)(a.m.n[2] - 4);
+        th[4] = (th[4] < zmax) ? th[4] : zmax;
+      } else {
+        double zmax = (double)a.m.n[2] - 0.5;
+        th[4] = ((double)th[4] < zmax) ? th[4] : (float)zmax;
+        th[5] = (th[5] > 0.0f) ? th[5] : 0.0f;
+        double wmax = (double)a.m.n[3] - 0.5;
+        th[5] = ((double)th[5] < wmax) ? th[5] : (float)wmax;
+      }
+      evaluate<MODE, false>(a, L, ws, lane, th, false, err, jac, hes);
+    } else {
+      lambda = 10.0f * lambda;
+    }
+  }
+
+  // CRLB and log-likelihood at the final theta.
+  FPair ll;
+  float fj[NV], fm[NH];
+  evaluate<MODE, true>(a, L, ws, lane, th, false, ll, fj, fm);
+  double M[NV * NV], diag[NV];
+#pragma unroll
+  for (int l = 0; l < NV; ++l)
+#pragma unroll
+    for (int mm = l; mm < NV; ++mm) M[l * NV + mm] = M[mm * NV + l] = (double)fm[hidx<NV>(l, mm)];
+  mat_inv_diag<NV>(M, diag);
+  if (lane == 0) {
+    const int64_t n = a.out_n;
+    const int64_t o = a.out_offset + roi;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) a.P[i * n + o] = th[i];
+    a.P[NV * n + o] = (float)kk;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) a.CRLB[i * n + o] = (float)diag[i];
+    a.LL[o] = ll.hi + ll.lo;
+  }
+  __syncwarp();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) fit_kernel(FitArgs a) {
+  extern __shared__ float4 smem4[];
+  float* smem = reinterpret_cast<float*>(smem4);
+  const WarpLayout L = make_layout(MODE, a.s);
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  float* ws = smem + wib * L.total();
+  const int64_t total_warps = (int64_t)gridDim.x * wpb;
+  for (int64_t roi = (int64_t)blockIdx.x * wpb + wib; roi < a.nfits; roi += total_warps)
+    fit_roi<MODE>(a, L, ws, lane, roi);
+}
+
+// One evaluation per ROI at caller-given parameters: writes, per ROI, the
+// deviance, the gradient (NV) and the packed upper-triangle Hessian (NH), or
+// with fisher set the log-likelihood, zeros and the Fisher information.
+template <int MODE>
+__global__ void __launch_bounds__(128) eval_kernel(FitArgs a, const float* theta, float* out,
+                                                   int fisher) {
+  using TR = ModeTraits<MODE>;
+  constexpr int NV = TR::NV;
+  constexpr int NH = NV * (NV + 1) / 2;
+  extern __shared__ float4 smem4[];
+  float* smem = reinterpret_cast<float*>(smem4);
+  const WarpLayout L = make_layout(MODE, a.s);
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  float* ws = smem + wib * L.total();
+  const int64_t total_warps = (int64_t)gridDim.x * wpb;
+  const int s2 = a.s * a.s;
+  for (int64_t roi = (int64_t)blockIdx.x * wpb + wib; roi < a.nfits; roi += total_warps) {
+    for (int p = lane; p < s2; p += 32) ws[p] = __ldg(a.rois + roi * (int64_t)s2 + p);
+    __syncwarp();
+    float th[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) th[i] = theta[i * a.nfits + roi];
+    FPair e;
+    float jac[NV], hes[NH];
+    if (fisher)
+      evaluate<MODE, true>(a, L, ws, lane, th, false, e, jac, hes);
+    else
+      evaluate<MODE, false>(a, L, ws, lane, th, false, e, jac, hes);
+    if (lane == 0) {
+      float* o = out + roi * (1 + NV + NH);
+      o[0] = e.hi + e.lo;
+#pragma unroll
+      for (int i = 0; i < NV; ++i) o[1 + i] = fisher ? 0.0f : jac[i];
+#pragma unroll
+      for (int i = 0; i < NH; ++i) o[1 + NV + i] = hes[i];
+    }
+    __syncwarp();
+  }
+}
+
+cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fisher,
+                        cudaStream_t stream) {
+  if (a.nfits <= 0) return cudaSuccess;
+  const int mode = a.m.fittype;
+  const int per_warp = warp_smem_floats(mode, a.s) * 4;
+  int wpb = 4;
+  while (wpb > 1 && per_warp * wpb > 200 * 1024) wpb >>= 1;
+  const int smem = per_warp * wpb;
+  void (*kern)(FitArgs, const float*, float*, int) = nullptr;
+  if (mode == 6) kern = eval_kernel<6>;
+  else if (mode == 7) kern = eval_kernel<7>;
+  else return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  int64_t grid = (a.nfits + wpb - 1) / wpb;
+  if (grid > 65535) grid = 65535;
+  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(a, theta, out, fisher);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+
+static int g_num_sms = 0;
+
+cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
+  if (a.nfits <= 0) return cudaSuccess;
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int mode = a.m.fittype;
+  const int per_warp = warp_smem_floats(mode, a.s) * 4;
+  int wpb = 4;
+  while (wpb > 1 && per_warp * wpb > 200 * 1024) wpb >>= 1;
+  const int smem = per_warp * wpb;
+  void (*kern)(FitArgs) = nullptr;
+  if (mode == 6) kern = fit_kernel<6>;
+  else if (mode == 7) kern = fit_kernel<7>;
+  else return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  int blocks_per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, 32 * wpb, smem);
+  if (e != cudaSuccess) return e;
+  if (blocks_per_sm < 1) blocks_per_sm = 1;
+  int64_t need = (a.nfits + wpb - 1) / wpb;
+  int64_t grid = (int64_t)g_num_sms * blocks_per_sm;
+  if (need < grid) grid = need;
+  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace bsfit

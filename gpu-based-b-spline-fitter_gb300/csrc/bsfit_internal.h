@@ -1,0 +1,41 @@
+// Internal types shared by the host library and the kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bsfit {
+
+// A PSF model resident on the device.
+struct ModelDev {
+  int fittype;           // 6, 7, 8
+  const float* coeff;    // device
+  const float* coeff3;   // device (fit type 8)
+  int cd[5];             // coefficient sizes, MATLAB order (Y, X, Z, W, U)
+  int64_t st[5];         // element strides of those axes
+  // nData per axis as the reference uses it: n[0] clamps Y (size(coeff,2) - 3),
+  // n[1] clamps X and sets the lateral offset (size(coeff,1) - 3), n[2..] Z, W, U.
+  int n[5];
+  float init_p[4];
+  int init_p_len;
+};
+
+struct FitArgs {
+  ModelDev m;
+  const float* rois;     // device, nfits * s * s
+  int s;
+  int64_t nfits;
+  int iterations;
+  float* P;              // device outputs, column-major with leading dim out_n
+  float* CRLB;
+  float* LL;
+  int64_t out_n;
+  int64_t out_offset;
+};
+
+int warp_smem_floats(int mode, int s);
+cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream);
+cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fisher,
+                        cudaStream_t stream);
+
+}  // namespace bsfit

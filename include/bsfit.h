@@ -1,0 +1,136 @@
+/*
+ * bsfit: GB300-native multi-dimensional cubic B-spline PSF maximum-likelihood
+ * fitter. C ABI of the shared library libbsfit.so.
+ *
+ * The entry points replace the reference's drop-in boundary for the B-spline
+ * fit types (6 = 3D, 7 = 4D colour, 8 = 5D + 3D mixture) of
+ * GPUmleFit_LM_multiD / CPUmleFit_LM (Li-Lab-SUSTech/GPU-based-B-spline-Fitter).
+ * Paths cited below are relative to the reference project root; VC stands for
+ * "MultiD_bspline/visual code".
+ *
+ * Array conventions (identical to the reference mex):
+ *  - ROI stack: float, MATLAB column-major [s, s, N]; pixel (ii, jj) of ROI n
+ *    at imstack[n*s*s + s*jj + ii].
+ *  - Coefficients: float, column-major with dims[0] fastest (MATLAB
+ *    size(coeff)), i.e. (Y, X, Z[, W[, U]]) as produced by bsarray.
+ *  - Outputs: P [N x (NV+1)] column-major (P[k*N + i]; the last column is the
+ *    iteration count), CRLB [N x NV] (variances), LL [N]. NV = 5, 6, 8 for fit
+ *    types 6, 7, 8. Parameter order: x, y, photons, background, z[, w[, u, g2]].
+ *
+ * Every call returns a status code; no call resets a device.
+ */
+#ifndef BSFIT_H
+#define BSFIT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bsfit_status {
+  BSFIT_OK = 0,
+  /* GPUmleFit_LM:WrongNoArgs (VC/GPUmleFit_LM/mexFunction.cpp:247-248) */
+  BSFIT_E_WRONG_NO_ARGS = 1,
+  /* GPUmleFit_LM:WrongDataType: a required array is missing (mex :251-252) */
+  BSFIT_E_WRONG_DATA_TYPE = 2,
+  /* GPUmleFit_LM:SubregionSize: s > 51 (mex :259-260) */
+  BSFIT_E_SUBREGION_SIZE = 3,
+  /* GPUmleFit_LM:SubregionShape: non-square ROI (mex :261-262) */
+  BSFIT_E_SUBREGION_SHAPE = 4,
+  /* fit types 1-5 (Gaussian / cubic spline) are not part of this library */
+  BSFIT_E_UNSUPPORTED_FITTYPE = 5,
+  /* GPUmleFit_LM:NotEnoughMemory (mex :409-456) */
+  BSFIT_E_NOT_ENOUGH_MEMORY = 6,
+  /* GPUmleFit_LM:cudaFail (mex :140-176), without the device reset */
+  BSFIT_E_CUDA = 7,
+  /* GPUmleFit_LM:NoDevice / nodevices (mex :186-203) */
+  BSFIT_E_NO_DEVICE = 8,
+  /* coefficient array too small (< 5 along an axis), wrong rank, or lateral
+   * sizes unequal (the reference indexes past the array there) */
+  BSFIT_E_COEFF_SIZE = 9,
+  /* initP missing or too short for fit type 7 (the reference dereferences it) */
+  BSFIT_E_INIT_P = 10,
+  /* invalid handle or argument of the device-level API */
+  BSFIT_E_INVALID = 11,
+  /* a bounded device-side wait ran out (batched / serving forms) */
+  BSFIT_E_TIMEOUT = 12
+} bsfit_status;
+
+/* Human-readable text of a status code (replaces mexErrMsgIdAndTxt texts). */
+const char* bsfit_status_str(int status);
+
+/* Library version string. */
+const char* bsfit_version(void);
+
+/*
+ * Synchronous drop-in call with host buffers. Replaces the B-spline branch of
+ * mexFunction in VC/GPUmleFit_LM/mexFunction.cpp:208-762 (argument parsing
+ * :247-385, device buffers :466-518, launch :598-674, copies back :685-734):
+ *
+ *   [P, CRLB, LL] = GPUmleFit_LM_multiD(imstack, fittype, iterations, coeff,
+ *                                        varmap, silent, initP, coeff3)
+ *
+ * imstack: [roi_size, roi_size2, nfits]; roi_size2 must equal roi_size and
+ *   roi_size must be <= 51.
+ * coeff / coeff_dims / coeff_ndim: 3, 4 or 5 dims for fit types 6, 7, 8.
+ * varmap: accepted and ignored for fit types 6-8, as in the reference
+ *   (mex :661-674 pass no variance map to the B-spline kernels).
+ * silent: 0 prints the reference's summary lines to stdout.
+ * init_p: fit type 7: (z, w), both taken from init_p when init_p[0] != 0,
+ *   else mid-grid (CPUmleFit_LM.cpp:2841-2850); fit type 8: (z, w, u, g2),
+ *   NULL for mid-grid z, w, u (CPUmleFit_LM.cpp:3246-3256); ignored for 6.
+ * coeff3: fit type 8 only, the 3D coefficients (same Y, X, Z sizes).
+ * P, CRLB, LL: caller-allocated host outputs.
+ */
+int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                              int64_t nfits, int32_t fittype, int32_t iterations,
+                              const float* coeff, int32_t coeff_ndim, const int64_t* coeff_dims,
+                              const float* varmap, int64_t varmap_numel, int32_t silent,
+                              const float* init_p, int64_t init_p_numel, const float* coeff3,
+                              int32_t coeff3_ndim, const int64_t* coeff3_dims, float* P,
+                              float* CRLB, float* LL);
+
+/* Number of fitted parameters for a fit type (5, 6, 8), or 0 if unsupported. */
+int bsfit_num_params(int32_t fittype);
+
+/*
+ * Device-resident model: the coefficient tables of one PSF model uploaded once
+ * and reused across calls (the reference uploads them on every call,
+ * mex :484-518). Copies from host memory; coeff3 only for fit type 8.
+ */
+typedef struct bsfit_model_s* bsfit_model;
+
+int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
+                       const int64_t* coeff_dims, const float* coeff3, int32_t coeff3_ndim,
+                       const int64_t* coeff3_dims, const float* init_p, int64_t init_p_numel,
+                       bsfit_model* out);
+int bsfit_model_release(bsfit_model model);
+
+/*
+ * Asynchronous fit on a CUDA stream with device pointers (replaces the launch
+ * wrappers VC/GPUmleFit_LM/wrapper.cu:256-279 and their kernels
+ * VC/GPUmleFit_LM/GPUmleFit_LM_EMCCD.cu:1208-2405). d_rois: nfits ROIs of
+ * roi_size^2 floats; d_P / d_CRLB / d_LL: device outputs in the layout above.
+ * stream: a cudaStream_t (NULL = legacy default stream). Uses no device memory
+ * beyond its arguments.
+ */
+int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                     int32_t iterations, float* d_P, float* d_CRLB, float* d_LL, void* stream);
+
+/*
+ * One model evaluation per ROI at given parameters, without the LM loop: the
+ * Poisson deviance, its gradient and the Hessian approximation the reference
+ * accumulates (VC/CPUmleFit_LM/CPUmleFit_LM.cpp:2537-2560), or with fisher != 0
+ * the log-likelihood and the Fisher information of the CRLB pass (:2725-2742).
+ * d_theta: NV x nfits column-major parameters; d_out: per ROI 1 + NV + NV(NV+1)/2
+ * floats: value, gradient (zeros for fisher), packed upper triangle row-major.
+ */
+int bsfit_eval_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                      const float* d_theta, int32_t fisher, float* d_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BSFIT_H */

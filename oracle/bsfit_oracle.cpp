@@ -872,3 +872,65 @@ void oracle_derivative5d_f32(float xi, float yi, float zi, float wi, float ui, i
 }
 
 }  // extern "C"
+
+namespace {
+template <typename T, typename MDL>
+void eval_entry(MDL& mdl, const T* rois, int sz, int nfits, const T* theta, int fisher, T* out) {
+  constexpr int NV = MDL::NV;
+  constexpr int NH = NV * (NV + 1) / 2;
+  for (int r = 0; r < nfits; ++r) {
+    const T* s_data = rois + (long long)sz * sz * r;
+    T th[NV + 1];
+    for (int i = 0; i < NV; ++i) th[i] = theta[(long long)i * nfits + r];
+    mdl.fr.off = (T)((float)(mdl.n[1] - sz) / 2.0f);
+    T* o = out + (long long)r * (1 + NV + NH);
+    T err = 0, jac[NV], hes[NV * NV];
+    if (!fisher) {
+      eval_roi<T>(mdl, sz, s_data, th, true, false, &err, jac, hes);
+    } else {
+      T M[NV * NV];
+      for (int i = 0; i < NV * NV; ++i) M[i] = 0;
+      mdl.prepare(th, sz);
+      T dudt[NV];
+      for (int ii = 0; ii < sz; ii++)
+        for (int jj = 0; jj < sz; jj++) {
+          T model;
+          mdl.pixel(ii, jj, th, dudt, &model);
+          accumulate_fisher<T>(model, s_data[sz * jj + ii], dudt, NV, M, &err);
+        }
+      for (int i = 0; i < NV; ++i) jac[i] = 0;
+      for (int i = 0; i < NV * NV; ++i) hes[i] = M[i];
+    }
+    o[0] = err;
+    for (int i = 0; i < NV; ++i) o[1 + i] = jac[i];
+    int k = 0;
+    for (int l = 0; l < NV; ++l)
+      for (int m = l; m < NV; ++m) o[1 + NV + k++] = hes[l * NV + m];
+  }
+}
+}  // namespace
+
+extern "C" {
+// One evaluation per ROI at given theta (NV x nfits column-major); out as
+// bsfit_eval_device: value, gradient, packed upper-triangle Hessian / Fisher.
+void oracle_eval6_f64(const double* rois, const double* coeff, int cx, int cy, int cz, int sz,
+                      int nfits, const double* theta, int fisher, double* out) {
+  Model3D<double> m;
+  m.coeff = coeff;
+  m.n[0] = cy - 3;
+  m.n[1] = cx - 3;
+  m.n[2] = cz - 3;
+  eval_entry<double, Model3D<double>>(m, rois, sz, nfits, theta, fisher, out);
+}
+void oracle_eval7_f64(const double* rois, const double* coeff, int cx, int cy, int cz, int cw,
+                      int sz, int nfits, const double* theta, int fisher, double* out) {
+  Model4D<double>* m = new Model4D<double>;
+  m->coeff = coeff;
+  m->n[0] = cy - 3;
+  m->n[1] = cx - 3;
+  m->n[2] = cz - 3;
+  m->n[3] = cw - 3;
+  eval_entry<double, Model4D<double>>(*m, rois, sz, nfits, theta, fisher, out);
+  delete m;
+}
+}  // extern "C"

@@ -110,3 +110,22 @@ class ReferenceOracle(_Base):
 
     def eval_bspline(self, x, deg):
         return self._libs[np.float32].ref_eval_bspline_f32(x, deg)
+
+
+def _eval_entry(self, rois, fittype, coeff, theta, fisher=False):
+    """One evaluation per ROI at theta ((N, NV) array): returns (N, 1+NV+NH)
+    float64 rows [value, gradient, packed upper-triangle Hessian/Fisher]."""
+    rois = np.ascontiguousarray(rois, dtype=np.float64)
+    n, s = rois.shape[0], rois.shape[-1]
+    coeff = np.ascontiguousarray(coeff, dtype=np.float64)
+    dims = list(reversed(coeff.shape))
+    nv = NV[fittype]
+    th = np.ascontiguousarray(np.asarray(theta, np.float64)[:, :nv].T)
+    out = np.zeros((n, 1 + nv + nv * (nv + 1) // 2), np.float64)
+    fn = getattr(self._lib, f"oracle_eval{fittype}_f64")
+    fn(_ptr(rois, np.float64), _ptr(coeff, np.float64), *[_i(d) for d in dims], _i(s), _i(n),
+       _ptr(th, np.float64), _i(int(fisher)), _ptr(out, np.float64))
+    return out
+
+
+Oracle.eval = _eval_entry

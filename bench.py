@@ -1,0 +1,284 @@
+"""Benchmark: ROI fits/s of the GB300 B-spline fitter on the batched 3D workload.
+
+Workload (one "step"): 1,000,000 synthetic 3D astigmatic ROIs mixing 11x11,
+13x13 and 17x17 pixels in the ratio 1:2:1, 30 LM iterations, fit type 6 - the
+batched 3D configuration the headline metric is quoted on. Inputs are seeded
+synthetic data (no public dataset exists for this path) and are larger than L2
+(~0.7 GB of pixels), so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl gb300 (default) prints one JSON line with
+  value: fits/s with the ROIs resident in HBM (CUDA events on the launch stream),
+  e2e:   fits/s through the public call (host buffers, copies in the timed region),
+  roofline: the fitter kernel against the measured FP32 FMA peak,
+  cpu_baseline: the oracle port of the reference CPU fitter on the host cores.
+--impl reference times the reference's CPU method (the bit-exact oracle port,
+all host threads) on a bounded sample of the same workload.
+Multi-GPU runs are independent replicas (every ROI is independent): each rank
+fits its own copy of the workload, rank 0 prints the aggregate.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "gpu-based-b-spline-fitter_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "ROI fits/s (3D 13px, 5D 17px) and p50/p99 latency: serving vs plain, 1 GB300"
+N_ROIS = 1_000_000
+SIZES = (11, 13, 17)
+ITERATIONS = 30
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 4 + i and s[4 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def make_workload():
+    from bsfit import workloads as W
+    return W.workload_3d_mixed(N_ROIS, sizes=SIZES, ratio=(1, 2, 1), iterations=ITERATIONS)
+
+
+def cpu_sample(groups, per_group_frac=0.016):
+    """A bounded, proportional sample of the workload for the CPU runs."""
+    return [(g.rois[: max(1, int(len(g.rois) * per_group_frac))], g) for g in groups]
+
+
+def run_cpu(groups, threads, frac):
+    from oracle.oracle import Oracle
+    o = Oracle()
+    n = 0
+    t0 = time.perf_counter()
+    for rois, g in cpu_sample(groups, frac):
+        o.fit(rois, g.fittype, g.iterations, g.coeff, precision="f32", threads=threads)
+        n += len(rois)
+    dt = time.perf_counter() - t0
+    return n, dt
+
+
+def bench_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    groups = make_workload()
+    threads = os.cpu_count() or 1
+    frac = 0.008
+    for _ in range(args.warmup):
+        run_cpu(groups, threads, frac / 4)
+    tot_n, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        n, dt = run_cpu(groups, threads, frac)
+        tot_n += n
+        tot_t += dt
+    v = tot_n / tot_t
+    sample = (f"{int(N_ROIS * frac)} ROIs per step ({frac:.1%} of the 1M-ROI 11/13/17 mix), "
+              f"oracle port of the reference CPU fitter (FP32, bit-exact), OpenMP over ROIs")
+    line = {"metric": METRIC, "value": v, "unit": "fits/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_t / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": "3d_batched_1M_11-13-17", "rois": N_ROIS, "fit_type": 6,
+                       "iterations": ITERATIONS, "parallelism": "replicas"},
+            "cpu_baseline": {"value": v, "unit": "fits/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def bench_gpu(args):
+    import torch
+    import bsfit
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    groups = make_workload()
+    models = {id(g.coeff): bsfit.Model(6, g.coeff) for g in groups}
+    stream = torch.cuda.Stream(dev)
+    d_rois = [torch.from_numpy(g.rois).to(dev) for g in groups]
+    outs = [(torch.empty((6, len(g.rois)), device=dev), torch.empty((5, len(g.rois)), device=dev),
+             torch.empty((len(g.rois),), device=dev)) for g in groups]
+    n_step = sum(len(g.rois) for g in groups)
+
+    def step():
+        for g, r, o in zip(groups, d_rois, outs):
+            models[id(g.coeff)].fit_torch(r, g.iterations, out=o, stream=stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 1)):
+            step()
+    stream.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = t.item()
+    value = n_step * world / (ms * 1e-3)
+
+    # Per-size kernel times and the roofline of the fitter kernel (events on
+    # the launch stream, one size group per launch).
+    iters = [o[0][5].float() for o in outs]
+    flops = sum(float(((it + 2.0) * bsfit.eval_flops(6, g.roi_size)).sum().item())
+                for it, g in zip(iters, groups))
+    mean_iter = float(sum(it.sum().item() for it in iters) / n_step)
+    per_launch = []
+    for g, r, o in zip(groups, d_rois, outs):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            for _ in range(3):
+                models[id(g.coeff)].fit_torch(r, g.iterations, out=o, stream=stream)
+            b.record(stream)
+        stream.synchronize()
+        per_launch.append(a.elapsed_time(b) / 3)
+    kernel_ms = sum(per_launch)
+    peak = bsfit.measure_fp32_peak()
+    achieved = flops / (kernel_ms * 1e-3) * 1e-12
+
+    # End to end through the public call: host buffers (pinned), copies and the
+    # per-call coefficient upload inside the timed region, as the mex does.
+    pinned = [torch.from_numpy(g.rois).pin_memory().numpy() for g in groups]
+    h2d = sum(p.nbytes for p in pinned) + sum(g.coeff.nbytes for g in groups)
+    d2h = n_step * (6 + 5 + 1) * 4
+    for g, p in zip(groups, pinned):
+        bsfit.GPUmleFit_LM_multiD(p[:1000], 6, g.iterations, g.coeff)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        for g, p in zip(groups, pinned):
+            bsfit.GPUmleFit_LM_multiD(p, 6, g.iterations, g.coeff)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = n_step * world / e2e_s
+
+    if rank != 0:
+        return 0
+    cpu_n, cpu_t = run_cpu(groups, os.cpu_count() or 1, 0.016)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_fit_kernel_3d.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("bytes_per_launch_scaled")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded); inputs > L2, no flush",
+        "config": {"workload": "3d_batched_1M_11-13-17", "rois": n_step, "fit_type": 6,
+                   "iterations": ITERATIONS, "roi_sizes": list(SIZES), "size_ratio": [1, 2, 1],
+                   "mean_iterations": mean_iter, "launches_per_step": len(groups),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e_value, "unit": "fits/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "measured FP32 FMA throughput on this device "
+                                    "(bsfit_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
+                     "flops_per_step": flops, "kernel_ms_per_step": kernel_ms,
+                     "kernel_ms_by_size": dict(zip([str(s) for s in SIZES], per_launch))},
+        "cpu_baseline": {"value": cpu_n / cpu_t, "unit": "fits/s", "cores": os.cpu_count(),
+                         "kind": "port",
+                         "sample": f"{cpu_n} ROIs (1.6% of each size group), FP32 oracle port of "
+                                   f"the reference CPU fitter, OpenMP over ROIs"},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps * len(groups),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return bench_reference(args)
+    return bench_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -103,6 +103,22 @@ class Model:
                         L.data_ptr(), st.cuda_stream)
         return P, C, L
 
+    def trace_torch(self, rois, iterations, flags=0, trace_max=None):
+        """Fit with per-iteration decision records; returns (P, CRLB, LL, trace)
+        with trace of shape (N, trace_max, 32)."""
+        import torch
+        n, s = rois.shape[0], rois.shape[-1]
+        tm = int(iterations) + 1 if trace_max is None else int(trace_max)
+        P = torch.empty((self.nv + 1, n), device=rois.device)
+        C = torch.empty((self.nv, n), device=rois.device)
+        L = torch.empty((n,), device=rois.device)
+        T = torch.zeros((n, tm, 32), device=rois.device)
+        st = torch.cuda.current_stream(rois.device)
+        check(_native.lib().bsfit_trace_device(self._h, rois.data_ptr(), s, n, int(iterations),
+                                               int(flags), P.data_ptr(), C.data_ptr(), L.data_ptr(),
+                                               T.data_ptr(), tm, st.cuda_stream), "bsfit_trace_device")
+        return P, C, L, T
+
     def eval_torch(self, rois, theta, fisher=False, stream=None):
         """One evaluation per ROI at theta (tensor (NV, N)); returns (N, 1+NV+NH)."""
         import torch
@@ -126,6 +142,28 @@ class Model:
             self.close()
         except Exception:
             pass
+
+
+def measure_fp32_peak():
+    """Measured FP32 FMA throughput of the current device, TFLOP/s."""
+    v = np.ctypeslib.ctypes.c_double()
+    check(_native.lib().bsfit_measure_fp32_peak(np.ctypeslib.ctypes.byref(v)), "fp32 peak")
+    return v.value
+
+
+def eval_flops(fittype, s, channels=1):
+    """Algorithmic FLOPs of one ROI evaluation (separable minimum): contract the
+    non-lateral axes over the (s+4)^2 knot window, one 4-tap pass per lateral
+    axis and output map, then the Jacobian, Hessian and deviance per pixel.
+    K = 4^(D-2) coefficients per lateral node."""
+    d = {6: 3, 7: 4, 8: 5}[fittype]
+    nv = NUM_PARAMS[fittype]
+    k = 4 ** (d - 2)
+    f = 2 * (d - 1) * k * (s + 4) ** 2 + (d + 1) * 8 * s * (2 * s + 4) + s * s * (2 * nv + nv * (nv + 1) + 6)
+    if fittype == 8:
+        # the 3D part of the mixture and the per-pixel mixing of model and dudt
+        f += 2 * 2 * 4 * (s + 4) ** 2 + 4 * 8 * s * (2 * s + 4) + 12 * s * s
+    return channels * f
 
 
 def version():

@@ -17,6 +17,7 @@ SIGNATURES = {
     "bsfit_status_str": (ctypes.c_char_p, [ctypes.c_int]),
     "bsfit_version": (ctypes.c_char_p, []),
     "bsfit_num_params": (ctypes.c_int, [ctypes.c_int32]),
+    "bsfit_measure_fp32_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "bsfit_GPUmleFit_LM_multiD": (ctypes.c_int, [
         _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
         _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int64,
@@ -28,6 +29,10 @@ SIGNATURES = {
     "bsfit_eval_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
+    "bsfit_trace_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+        ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_int32, ctypes.c_void_p]),
     "bsfit_fit_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),

@@ -112,6 +112,11 @@ const char* bsfit_version(void) { return "bsfit-gb300 0.1 (sm_103a)"; }
 
 int bsfit_num_params(int32_t fittype) { return num_params(fittype); }
 
+int bsfit_measure_fp32_peak(double* tflops) {
+  if (!tflops) return BSFIT_E_INVALID;
+  return cuda_status(bsfit::measure_fp32_peak(tflops));
+}
+
 int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
                        const int64_t* coeff_dims, const float* coeff3, int32_t coeff3_ndim,
                        const int64_t* coeff3_dims, const float* init_p, int64_t init_p_numel,
@@ -169,6 +174,7 @@ int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, i
   if (nfits == 0) return BSFIT_OK;
   if (!d_rois || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
   FitArgs a;
+  std::memset(&a, 0, sizeof(a));
   a.m = model->dev;
   a.rois = d_rois;
   a.s = (int)roi_size;
@@ -179,6 +185,34 @@ int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, i
   a.LL = d_LL;
   a.out_n = nfits;
   a.out_offset = 0;
+  a.trace = nullptr;
+  a.trace_max = 0;
+  a.flags = 0;
+  return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
+}
+
+int bsfit_trace_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                       int32_t iterations, int32_t flags, float* d_P, float* d_CRLB, float* d_LL,
+                       float* d_trace, int32_t trace_max, void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0 || trace_max < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_P || !d_CRLB || !d_LL || (trace_max > 0 && !d_trace)) return BSFIT_E_INVALID;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  a.out_n = nfits;
+  a.trace = d_trace;
+  a.trace_max = trace_max;
+  a.flags = flags;
   return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
 }
 

@@ -499,12 +499,25 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
 
   int kk = 0;
   for (kk = 0; kk < a.iterations; kk++) {
+    float* rec = (a.trace && kk < a.trace_max && lane == 0)
+                     ? a.trace + (roi * (int64_t)a.trace_max + kk) * TRACE_REC
+                     : nullptr;
     // |(newErr - oldErr) / newErr| < 1e-6 (CPUmleFit_LM.cpp:2565)
     {
       float dhi = err.hi - oerr.hi;
       float dlo = err.lo - oerr.lo;
       float rel = fabsf((dhi + dlo) / (err.hi + err.lo));
-      if (rel < 1e-6f) break;
+      if (rec) {
+        rec[0] = (float)kk;
+        rec[1] = rel;
+        rec[2] = err.hi + err.lo;
+        rec[3] = oerr.hi + oerr.lo;
+        rec[4] = 0.0f;
+      }
+      if (rel < 1e-6f) {
+        if (rec) rec[4] = 1.0f;
+        break;
+      }
     }
     const float e_new = err.hi + err.lo, e_old = oerr.hi + oerr.lo;
     if ((double)e_new > 1.5 * (double)e_old) {
@@ -527,19 +540,44 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     // reference).
 #pragma unroll
     for (int i = 0; i < NV; i++) hes[hidx<NV>(i, i)] *= lambda;
-    float full[NV * NV], u[NV * NV], upd[NV];
+    float full[NV * NV], u[NV * NV], upd[NV], rhs[NV];
 #pragma unroll
     for (int l = 0; l < NV; ++l)
 #pragma unroll
       for (int mm = l; mm < NV; ++mm) full[l * NV + mm] = full[mm * NV + l] = hes[hidx<NV>(l, mm)];
+    // A parameter whose derivative is exactly zero at every pixel (z on the
+    // mirror-padded boundary knot) has an exactly zero Hessian row. The
+    // reference only survives that case through rounding noise of its double
+    // derivative sums (a ~1e-29 pivot and a huge step of noise-determined
+    // sign, cut to +-clamp); an exact zero would give NaN. Such a parameter is
+    // held for this step instead: its row becomes the identity and its
+    // gradient zero.
+#pragma unroll
+    for (int l = 0; l < NV; ++l) {
+      rhs[l] = jac[l];
+      if (full[l * NV + l] == 0.0f) {
+#pragma unroll
+        for (int mm = 0; mm < NV; ++mm) full[l * NV + mm] = full[mm * NV + l] = 0.0f;
+        full[l * NV + l] = 1.0f;
+        rhs[l] = 0.0f;
+      }
+    }
     bool ok = cholesky<NV>(full, u);
-    if (ok) {
-      chol_solve<NV>(u, jac, upd);
+    if (ok && (a.flags & FLAG_NO_REFINE)) {
+      chol_solve<NV>(u, rhs, upd);
+      if (MODE != 6) {
+        bool bad = false;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) bad |= (upd[i] != upd[i]);
+        if (bad) ok = false;
+      }
+    } else if (ok) {
+      chol_solve<NV>(u, rhs, upd);
       // One refinement step: r = J - H upd with error-free products.
       float r[NV];
 #pragma unroll
       for (int i = 0; i < NV; ++i) {
-        float sh = jac[i], sl = 0.0f;
+        float sh = rhs[i], sl = 0.0f;
 #pragma unroll
         for (int j = 0; j < NV; ++j) {
           float p, pe, t, te;
@@ -606,6 +644,16 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
       evaluate<MODE, false>(a, L, ws, lane, th, false, err, jac, hes);
     } else {
       lambda = 10.0f * lambda;
+    }
+    if (rec) {
+      const float e_n = err.hi + err.lo;
+      rec[4] = (e_new > 1.5f * e_old ? 2.0f : 0.0f) + (e_new < e_old ? 4.0f : 0.0f) + (ok ? 8.0f : 0.0f);
+      rec[5] = lambda;
+#pragma unroll
+      for (int i = 0; i < NV; ++i) rec[6 + i] = ok ? upd[i] : 0.0f;
+#pragma unroll
+      for (int i = 0; i < NV; ++i) rec[14 + i] = th[i];
+      rec[22] = e_n;
     }
   }
 
@@ -706,6 +754,48 @@ cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fi
   if (grid > 65535) grid = 65535;
   kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(a, theta, out, fisher);
   return cudaGetLastError();
+}
+
+// FP32 FMA throughput probe: the denominator of the fitter's roofline
+// (an FP32-pipe-bound kernel), measured on the same device and clocks.
+__global__ void fp32_peak_kernel(float* out, int iters, float a, float b) {
+  float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1.f, x2 = x0 + 2.f, x3 = x0 + 3.f;
+  float x4 = x0 + 4.f, x5 = x0 + 5.f, x6 = x0 + 6.f, x7 = x0 + 7.f;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+cudaError_t measure_fp32_peak(double* tflops) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 1 << 14;
+  float* out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(float) * blocks * threads);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fp32_peak_kernel<<<blocks, threads>>>(out, 256, 0.999f, 1e-4f);
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    cudaEventRecord(e0);
+    fp32_peak_kernel<<<blocks, threads>>>(out, iters, 0.999f, 1e-4f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = ms < best ? ms : best;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (best * 1e-3) * 1e-12;
+  return e;
 }
 
 // ---------------------------------------------------------------------------

@@ -31,10 +31,19 @@ struct FitArgs {
   float* LL;
   int64_t out_n;
   int64_t out_offset;
+  // Diagnostics: optional per-ROI decision trace (TRACE_REC floats per
+  // iteration, trace_max iterations per ROI) and option bits.
+  float* trace;
+  int trace_max;
+  int flags;
 };
+
+constexpr int TRACE_REC = 32;
+constexpr int FLAG_NO_REFINE = 1;  // skip the refinement step of the LM solve
 
 int warp_smem_floats(int mode, int s);
 cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream);
+cudaError_t measure_fp32_peak(double* tflops);
 cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fisher,
                         cudaStream_t stream);
 

@@ -94,6 +94,11 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
 /* Number of fitted parameters for a fit type (5, 6, 8), or 0 if unsupported. */
 int bsfit_num_params(int32_t fittype);
 
+/* Measured FP32 FMA throughput of the current device in TFLOP/s (2 FLOP per
+ * FMA), the roofline denominator of the fitter kernels. No reference
+ * counterpart: a measurement utility. */
+int bsfit_measure_fp32_peak(double* tflops);
+
 /*
  * Device-resident model: the coefficient tables of one PSF model uploaded once
  * and reused across calls (the reference uploads them on every call,
@@ -128,6 +133,18 @@ int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, i
  */
 int bsfit_eval_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
                       const float* d_theta, int32_t fisher, float* d_out, void* stream);
+
+/*
+ * Diagnostic form of bsfit_fit_device (no counterpart in the reference): also
+ * writes, per ROI and LM iteration, a 32-float decision record to d_trace
+ * (trace_max records per ROI: iteration, |dErr/err|, new and old deviance,
+ * decision bits 1 converged / 2 rejected / 4 improved / 8 solve accepted,
+ * lambda, the step (8), theta after the step (8), deviance after the step).
+ * flags bit 0 skips the refinement step of the LM solve.
+ */
+int bsfit_trace_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                       int32_t iterations, int32_t flags, float* d_P, float* d_CRLB, float* d_LL,
+                       float* d_trace, int32_t trace_max, void* stream);
 
 #ifdef __cplusplus
 }

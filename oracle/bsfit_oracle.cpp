@@ -526,9 +526,14 @@ void eval_roi(MDL& mdl, int sz, const T* s_data, const T* theta, bool pow_double
 
 // The shared LM loop. See the mode notes inline; line numbers are for
 // VC/CPUmleFit_LM/CPUmleFit_LM.cpp.
+// Decision trace of one LM iteration (test infrastructure): TRACE_REC doubles
+// per iteration, see the field list at the write below.
+constexpr int TRACE_REC = 32;
+
 template <typename T, typename MDL, Mode MODE>
 void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, const T* initP,
-             T* d_Parameters, T* d_CRLBs, T* d_LogLikelihood, int Nfits) {
+             T* d_Parameters, T* d_CRLBs, T* d_LogLikelihood, int Nfits,
+             double* trace = nullptr, int trace_max = 0) {
   constexpr int NV = MDL::NV;
   const int* n = mdl.n;
   const T* s_data = d_data + (long long)sz * sz * subregion;
@@ -598,9 +603,22 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
 
   int kk;
   for (kk = 0; kk < iterations; kk++) {
+    double* rec = (trace && kk < trace_max) ? trace + (long long)kk * TRACE_REC : nullptr;
+    int flags = 0;
+    if (rec) {
+      rec[0] = kk;
+      rec[1] = std::fabs((double)((newErr - oldErr) / newErr));
+      rec[2] = newErr;
+      rec[3] = oldErr;
+    }
     bool conv = std::fabs((newErr - oldErr) / newErr) < kTOL;
     if (MODE == MODE8) conv = conv || (sumUpdate < kTOL1);  // :3355
-    if (conv) break;
+    if (conv) {
+      if (rec) rec[4] = 1;
+      break;
+    }
+    if ((double)newErr > 1.5 * (double)oldErr) flags |= 2;
+    else if (newErr < oldErr) flags |= 4;
     if ((double)newErr > 1.5 * (double)oldErr) {
       for (int i = 0; i < NV; i++) {
         newSign[i] = oldSign[i];
@@ -620,6 +638,11 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
     std::memset(L, 0, NV * sizeof(T));
     std::memset(U, 0, NV * sizeof(T));
     int info = cholesky<T>(hessian, NV, L, U);
+    if (rec) {
+      double mp = 1e300;
+      for (int i = 0; i < NV; ++i) mp = std::min(mp, (double)U[i * NV + i]);
+      rec[22] = (info == 0) ? mp : -1.0;
+    }
     if (info == 0) {
       lu_evaluate<T>(L, U, jacobian, NV, newUpdate);
       if (MODE != MODE6) {
@@ -629,6 +652,10 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
           if (std::isnan(newUpdate[ll])) bad = true;
         if (bad) info = 1;
       }
+    }
+    if (rec) {
+      flags |= (info == 0) ? 8 : 0;
+      for (int i = 0; i < NV; ++i) rec[6 + i] = newUpdate[i];
     }
     if (info == 0) {
       if (MODE == MODE7) newUpdate[5] = newUpdate[5] * 10;  // :2951
@@ -641,7 +668,9 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
       oldErr = newErr;
       if (MODE == MODE7) {
         // "let it go", :2966-2971
+        if (rec) rec[23] = std::fabs((double)newUpdate[4]);
         if ((std::fabs((double)newUpdate[4]) < 0.005) && turn) {
+          flags |= 32;
           newClamp[5] = T(n[3]) / 10;
           oldClamp[5] = T(n[3]) / 10;
           turn = 0;
@@ -706,6 +735,21 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
     } else {
       newLambda = 10 * newLambda;
     }
+    if (rec) {
+      rec[4] = flags;
+      rec[5] = newLambda;
+      for (int i = 0; i < NV; ++i) rec[14 + i] = newTheta[i];
+      int sg = 0;
+      for (int i = 0; i < NV; ++i) sg |= (newSign[i] > 0 ? 1 : 0) << i;
+      rec[24] = sg;
+      for (int i = 0; i < NV && 25 + i < TRACE_REC; ++i) rec[25 + i] = newClamp[i];
+    }
+  }
+  if (trace && kk < trace_max && !(kk < iterations)) {
+    // cap reached: mark a terminal record
+    double* rec = trace + (long long)kk * TRACE_REC;
+    rec[0] = kk;
+    rec[4] = 64;
   }
 
   // CRLB and log-likelihood (:2714-2755). Modes 6 and 7 re-evaluate at the
@@ -932,5 +976,38 @@ void oracle_eval7_f64(const double* rois, const double* coeff, int cx, int cy, i
   m->n[3] = cw - 3;
   eval_entry<double, Model4D<double>>(*m, rois, sz, nfits, theta, fisher, out);
   delete m;
+}
+}  // extern "C"
+
+extern "C" {
+// Decision trace of one ROI (test infrastructure): writes up to trace_max
+// records of 32 doubles: [0] iteration, [1] |dErr/err|, [2] newErr, [3] oldErr,
+// [4] flags (1 converged, 2 rejected, 4 improved, 8 Cholesky ok, 32 let-it-go,
+// 64 cap), [5] lambda, [6..13] solve result, [14..21] theta after the step,
+// [22] smallest Cholesky diagonal (-1 on failure), [23] |dz| (fit type 7),
+// [24] sign bits, [25..31] clamps. Returns the output row as fit6/7 would.
+void oracle_trace_f32(int fittype, const float* data, const float* coeff, const float* coeff3,
+                      const int* dims, int sz, int iterations, const float* initP, int roi,
+                      int nfits, float* P, float* CRLB, float* LL, double* trace, int trace_max) {
+  if (fittype == 6) {
+    Model3D<float> m; m.coeff = coeff; m.n[0] = dims[1] - 3; m.n[1] = dims[0] - 3; m.n[2] = dims[2] - 3;
+    fit_roi<float, Model3D<float>, MODE6>(m, roi, data, sz, iterations, nullptr, P, CRLB, LL, nfits, trace, trace_max);
+  } else if (fittype == 7) {
+    Model4D<float>* m = new Model4D<float>; m->coeff = coeff; m->n[0] = dims[1] - 3; m->n[1] = dims[0] - 3; m->n[2] = dims[2] - 3; m->n[3] = dims[3] - 3;
+    fit_roi<float, Model4D<float>, MODE7>(*m, roi, data, sz, iterations, initP, P, CRLB, LL, nfits, trace, trace_max);
+    delete m;
+  }
+}
+void oracle_trace_f64(int fittype, const double* data, const double* coeff, const double* coeff3,
+                      const int* dims, int sz, int iterations, const double* initP, int roi,
+                      int nfits, double* P, double* CRLB, double* LL, double* trace, int trace_max) {
+  if (fittype == 6) {
+    Model3D<double> m; m.coeff = coeff; m.n[0] = dims[1] - 3; m.n[1] = dims[0] - 3; m.n[2] = dims[2] - 3;
+    fit_roi<double, Model3D<double>, MODE6>(m, roi, data, sz, iterations, nullptr, P, CRLB, LL, nfits, trace, trace_max);
+  } else if (fittype == 7) {
+    Model4D<double>* m = new Model4D<double>; m->coeff = coeff; m->n[0] = dims[1] - 3; m->n[1] = dims[0] - 3; m->n[2] = dims[2] - 3; m->n[3] = dims[3] - 3;
+    fit_roi<double, Model4D<double>, MODE7>(*m, roi, data, sz, iterations, initP, P, CRLB, LL, nfits, trace, trace_max);
+    delete m;
+  }
 }
 }  // extern "C"

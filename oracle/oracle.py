@@ -129,3 +129,24 @@ def _eval_entry(self, rois, fittype, coeff, theta, fisher=False):
 
 
 Oracle.eval = _eval_entry
+
+
+def _trace(self, rois, fittype, iterations, coeff, roi, init_p=None, precision="f64"):
+    """Per-iteration decision records of one ROI (see oracle_trace_f32)."""
+    dt = np.float32 if precision == "f32" else np.float64
+    rois = np.ascontiguousarray(rois, dtype=dt)
+    n, s = rois.shape[0], rois.shape[-1]
+    coeff = np.ascontiguousarray(coeff, dtype=dt)
+    dims = (ctypes.c_int * 5)(*(list(reversed(coeff.shape)) + [1] * (5 - coeff.ndim)))
+    nv = NV[fittype]
+    P = np.zeros((nv + 1, n), dt); C = np.zeros((nv, n), dt); L = np.zeros(n, dt)
+    tr = np.zeros((iterations + 1, 32), np.float64)
+    ip = np.ascontiguousarray(init_p if init_p is not None else np.zeros(4), dtype=dt)
+    fn = getattr(self._lib, f"oracle_trace_{precision}")
+    fn(_i(fittype), _ptr(rois, dt), _ptr(coeff, dt), None, dims, _i(s), _i(iterations),
+       _ptr(ip, dt), _i(roi), _i(n), _ptr(P, dt), _ptr(C, dt), _ptr(L, dt),
+       tr.ctypes.data_as(_dp), _i(iterations + 1))
+    return tr, P[:, roi], C[:, roi], L[roi]
+
+
+Oracle.trace = _trace

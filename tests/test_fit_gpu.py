@@ -1,0 +1,195 @@
+"""GPU parity of the CUDA fitter against the reference method.
+
+Checks, through the C ABI on cuda:0:
+  * the golden fixtures (outputs of the reference's own CPU fitter, FP32 and
+    FP64 builds) and the oracle on the GPU machine;
+  * seeded workloads at scale against the FP64 oracle, per ROI, with the
+    tolerances of the reference method's precision budget:
+        x, y within 1e-4 px; z within 1e-2 nm (5e-4 knot units on the 20 nm
+        grid); photons and background within 1e-5 relative; extra dimensions
+        within 1e-4; CRLB within 1e-4 relative (both "unidentifiable", i.e.
+        > 1e25 or inf, also counts as agreement).
+The LM trajectory of the reference method has discrete decisions (convergence
+threshold, update-sign clamp halving, accept/reject, the 4D "let it go"
+switch); rounding differences flip some of them, after which a ROI can end
+elsewhere. The reference's own FP32 build differs from its FP64 build on such
+ROIs too. The tests therefore bound the per-ROI pass fraction and require the
+GPU to be at least as close to the FP64 oracle as the reference's FP32 build.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cases
+
+pytestmark = pytest.mark.gpu
+
+Z_NM_PER_UNIT = 20.0
+
+
+def tol_pass(P, C, R, RC, nv, z_nm=Z_NM_PER_UNIT):
+    ok = np.abs(P[:, :2] - R[:, :2]).max(1) <= 1e-4
+    ok &= np.abs(P[:, 4] - R[:, 4]) * z_nm <= 1e-2
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ok &= np.abs(P[:, 2] / R[:, 2] - 1) <= 1e-5
+        ok &= np.abs(P[:, 3] / R[:, 3] - 1) <= 1e-5
+        for k in range(5, nv):
+            ok &= np.abs(P[:, k] - R[:, k]) <= 1e-4
+        big_r = (RC > 1e25) | ~np.isfinite(RC)
+        big_c = (C > 1e25) | ~np.isfinite(C)
+        relc = np.abs(C / RC - 1)
+        relc[big_r & big_c] = 0
+        ok &= (relc <= 1e-4).all(1)
+    return ok
+
+
+@pytest.fixture(scope="module")
+def bsfit_mod():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import __graft_entry__
+    __graft_entry__.build()
+    import bsfit
+    return bsfit
+
+
+def _fit(bsfit_mod, d):
+    kw = {}
+    if "init_p" in d:
+        kw["initP"] = d["init_p"]
+    if "coeff3" in d:
+        kw["coeff3"] = d["coeff3"]
+    return bsfit_mod.GPUmleFit_LM_multiD(d["rois"], int(d["fittype"]), int(d["iterations"]),
+                                         d["coeff"], **kw)
+
+
+def degenerate_rois(oracle, d):
+    """ROIs whose FP64 reference trajectory passes through a (near-)singular
+    Hessian: a solve step larger than 1e4 in x, y or z. There the reference's
+    next move is decided by rounding noise of its double derivative sums
+    (a tiny pivot, a huge step of noise-determined sign, cut to +-clamp), which
+    no other arithmetic reproduces."""
+    ft = int(d["fittype"])
+    kw = {"init_p": d["init_p"]} if "init_p" in d else {}
+    out = np.zeros(len(d["rois"]), bool)
+    for r in range(len(d["rois"])):
+        tr, *_ = oracle.trace(d["rois"], ft, int(d["iterations"]), d["coeff"], r, precision="f64",
+                              **kw)
+        steps = tr[:, [6, 7, 10]]
+        out[r] = bool(np.any(np.abs(steps) > 1e4))
+    return out
+
+
+@pytest.mark.parametrize("case", [c for c in golden_cases() if not c.startswith("m8")])
+def test_golden_fixture(bsfit_mod, oracle, case):
+    d = np.load(os.path.join(GOLDEN, case + ".npz"))
+    ft = int(d["fittype"])
+    nv = {6: 5, 7: 6, 8: 8}[ft]
+    P, C, L = _fit(bsfit_mod, d)
+    n = len(d["rois"])
+    assert P.shape == (n, nv + 1) and C.shape == (n, nv) and L.shape == (n,)
+    # the oracle on this machine still reproduces the reference's fixture
+    kw = {k: d[k] for k in ("init_p", "coeff3") if k in d}
+    Po, Co, Lo = oracle.fit(d["rois"], ft, int(d["iterations"]), d["coeff"], precision="f64", **kw)
+    assert np.array_equal(Po, d["f64_P"], equal_nan=True)
+    R, RC = d["f64_P"], d["f64_CRLB"]
+    finite = np.isfinite(R).all(1)
+    if int(d["iterations"]) == 0:
+        # no LM step: the initial guesses and the CRLB pass only
+        np.testing.assert_allclose(P[finite], R[finite].astype(np.float32), rtol=1e-5, atol=1e-5)
+        return
+    ok = tol_pass(P, C, R, RC, nv)
+    ok32 = tol_pass(d["f32_P"], d["f32_CRLB"], R, RC, nv)
+    keep = ~degenerate_rois(oracle, d) & finite
+    # On ROIs with a regular reference trajectory: at least as close to the
+    # FP64 reference as the reference's FP32 build, with one ROI in 8 of slack
+    # for these small cases (one in 4 for fit type 7, whose "let it go" switch
+    # and 1e-5 initial w clamp make its trajectory far more rounding-sensitive:
+    # the reference's own FP32 and FP64 builds agree on only a third of 4D ROIs).
+    slack = max(1, keep.sum() // (4 if ft == 7 else 8))
+    assert ok[keep].sum() >= ok32[keep].sum() - slack, (
+        case, ok[keep].mean(), ok32[keep].mean(), np.where(keep & ~ok)[0])
+    # Iteration counts are integers in the last column.
+    assert np.all(P[:, nv] == np.round(P[:, nv])) and np.all(P[:, nv] <= int(d["iterations"]))
+
+
+def test_special_rois_no_crash(bsfit_mod):
+    """All-zero, negative, single-pixel and constant ROIs (m6_edges tail):
+    finite where the reference is finite, NaN where it is NaN."""
+    d = np.load(os.path.join(GOLDEN, "m6_edges.npz"))
+    P, C, L = _fit(bsfit_mod, d)
+    R = d["f64_P"]
+    assert np.array_equal(np.isnan(P[:, :5]), np.isnan(R[:, :5]))
+
+
+@pytest.mark.parametrize("fittype,n,min_frac", [(6, 20000, 0.955), (7, 3000, 0.33)])
+def test_parity_at_scale(bsfit_mod, oracle, fittype, n, min_frac):
+    from bsfit import workloads as W
+    if fittype == 6:
+        wl = W.workload_3d(n, s=13, stream=501)
+    else:
+        wl = W.workload_4d(n, sizes=(13,), stream=502)[0]
+    nv = {6: 5, 7: 6}[fittype]
+    kw = {"initP": wl.init_p} if wl.init_p is not None else {}
+    P, C, L = bsfit_mod.GPUmleFit_LM_multiD(wl.rois, fittype, wl.iterations, wl.coeff, **kw)
+    threads = os.cpu_count() or 1
+    R, RC, RL = oracle.fit(wl.rois, fittype, wl.iterations, wl.coeff, init_p=wl.init_p,
+                           precision="f64", threads=threads)
+    S, SC, SL = oracle.fit(wl.rois, fittype, wl.iterations, wl.coeff, init_p=wl.init_p,
+                           precision="f32", threads=threads)
+    ok = tol_pass(P, C, R, RC, nv)
+    ok32 = tol_pass(S, SC, R, RC, nv)
+    assert ok.mean() >= min_frac, ok.mean()
+    assert ok.mean() >= ok32.mean() - 0.02, (ok.mean(), ok32.mean())
+    # Typical accuracy: 3D far inside the tolerances; 4D at the level of the
+    # reference's own FP32 build (median |dz| 1.6e-3 nm against FP64).
+    assert np.median(np.abs(P[:, 0] - R[:, 0])) < 1e-5
+    zmed = np.median(np.abs(P[:, 4] - R[:, 4])) * Z_NM_PER_UNIT
+    zmed32 = np.median(np.abs(S[:, 4] - R[:, 4])) * Z_NM_PER_UNIT
+    assert zmed < (1e-3 if fittype == 6 else 2 * zmed32 + 1e-3), (zmed, zmed32)
+    assert np.median(np.abs(C / RC - 1)) < (1e-4 if fittype == 6 else 1e-3)
+    assert np.median(np.abs(L - RL)) < 1e-3
+
+
+def test_fit_device_matches_host_call(bsfit_mod):
+    """The device-pointer entry point gives the same results as the host call."""
+    import torch
+    d = np.load(os.path.join(GOLDEN, "m6_basic.npz"))
+    P, C, L = _fit(bsfit_mod, d)
+    m = bsfit_mod.Model(6, d["coeff"])
+    r = torch.from_numpy(d["rois"]).cuda()
+    Pd, Cd, Ld = m.fit_torch(r, int(d["iterations"]))
+    torch.cuda.synchronize()
+    assert np.array_equal(Pd.cpu().numpy().T, P)
+    assert np.array_equal(Cd.cpu().numpy().T, C)
+    assert np.array_equal(Ld.cpu().numpy(), L)
+
+
+def test_eval_matches_oracle_at_fixed_parameters(bsfit_mod, oracle):
+    """One evaluation at the reference's final parameters: deviance, gradient,
+    Hessian and Fisher information, trajectory-free. Gradient entry k is
+    compared in units of sqrt(H_kk), Hessian entry (k, l) in units of
+    sqrt(H_kk H_ll) (with a floor of 1e-6 of the column median, so an
+    identically zero curvature on a boundary knot does not divide by zero)."""
+    import torch
+    for case in ("m6_basic", "m7_basic"):
+        d = np.load(os.path.join(GOLDEN, case + ".npz"))
+        ft = int(d["fittype"])
+        nv = {6: 5, 7: 6}[ft]
+        theta = d["f64_P"][:, :nv].astype(np.float32)
+        m = bsfit_mod.Model(ft, d["coeff"], init_p=d["init_p"] if "init_p" in d else None)
+        r = torch.from_numpy(d["rois"]).cuda()
+        th = torch.from_numpy(np.ascontiguousarray(theta.T)).cuda()
+        idx = [(l, k) for l in range(nv) for k in range(l, nv)]
+        for fisher in (False, True):
+            g = m.eval_torch(r, th, fisher=fisher).cpu().numpy().astype(np.float64)
+            ref = oracle.eval(d["rois"], ft, d["coeff"], theta.astype(np.float64), fisher=fisher)
+            diag = np.stack([ref[:, 1 + nv + idx.index((k, k))] for k in range(nv)], 1)
+            diag = np.maximum(diag, 1e-6 * np.median(diag, 0))
+            e0 = np.abs(g[:, 0] - ref[:, 0]).max() / np.abs(ref[:, 0]).max()
+            eJ = (np.abs(g[:, 1:1 + nv] - ref[:, 1:1 + nv]) / np.sqrt(diag)).max()
+            eH = max((np.abs(g[:, 1 + nv + i] - ref[:, 1 + nv + i]) /
+                      np.sqrt(diag[:, l] * diag[:, k])).max() for i, (l, k) in enumerate(idx))
+            assert e0 < 1e-5 and eJ < 1e-3 and eH < 1e-3, (case, fisher, e0, eJ, eH)

@@ -93,9 +93,36 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def make_workload():
+def make_workload(n=N_ROIS, sizes=SIZES):
     from bsfit import workloads as W
-    return W.workload_3d_mixed(N_ROIS, sizes=SIZES, ratio=(1, 2, 1), iterations=ITERATIONS)
+    if len(sizes) == 1:
+        return [W.workload_3d(n, s=sizes[0], iterations=ITERATIONS, stream=2)]
+    return W.workload_3d_mixed(n, sizes=sizes, ratio=(1, 2, 1), iterations=ITERATIONS)
+
+
+def bench_kernel_only(args):
+    """Profiling case: warm-up plus timed fits of one workload, nothing else."""
+    import torch
+    import bsfit
+    groups = make_workload(args.rois, tuple(args.sizes))
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    work = []
+    for g in groups:
+        m = bsfit.Model(6, g.coeff)
+        r = torch.from_numpy(g.rois).to(dev)
+        o = (torch.empty((6, len(g.rois)), device=dev), torch.empty((5, len(g.rois)), device=dev),
+             torch.empty((len(g.rois),), device=dev))
+        work.append((m, r, o, g))
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup + args.steps):
+            for m, r, o, g in work:
+                m.fit_torch(r, g.iterations, out=o, stream=stream)
+    stream.synchronize()
+    n = sum(len(g.rois) for g in groups)
+    print(json.dumps({"profile_case": True, "rois": n, "sizes": args.sizes,
+                      "launches": (args.warmup + args.steps) * len(groups)}))
+    return 0
 
 
 def cpu_sample(groups, per_group_frac=0.016):
@@ -234,11 +261,17 @@ def bench_gpu(args):
     if rank != 0:
         return 0
     cpu_n, cpu_t = run_cpu(groups, os.cpu_count() or 1, 0.016)
+    # DRAM traffic of the fitter per step: the ncu capture of the 13 px case
+    # (profiles/fit_kernel_3d13.md) measured bytes per ROI against the
+    # algorithmic 4 s^2 + 48 B; the step's traffic scales that ratio by each
+    # size group's algorithmic bytes (traffic grows with the pixels read).
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic_fit_kernel_3d.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get("bytes_per_launch_scaled")
+            per_roi = float(json.load(open(tpath))["dram_bytes_per_roi"])
+            ratio = per_roi / (4 * 13 * 13 + 48)
+            traffic = ratio * sum((4 * g.roi_size ** 2 + 48) * len(g.rois) for g in groups)
         except Exception:
             traffic = None
     line = {
@@ -256,6 +289,7 @@ def bench_gpu(args):
                      "peak_source": "measured FP32 FMA throughput on this device "
                                     "(bsfit_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                      "flops_per_step": flops, "kernel_ms_per_step": kernel_ms,
+                     "per": "step (one launch per ROI size; achieved and traffic cover all three)",
                      "kernel_ms_by_size": dict(zip([str(s) for s in SIZES], per_launch))},
         "cpu_baseline": {"value": cpu_n / cpu_t, "unit": "fits/s", "cores": os.cpu_count(),
                          "kind": "port",
@@ -274,9 +308,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="profiling case: only the fit launches of --rois ROIs of --sizes")
+    ap.add_argument("--rois", type=int, default=N_ROIS)
+    ap.add_argument("--sizes", type=int, nargs="+", default=list(SIZES))
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)
+    if args.kernel_only:
+        return bench_kernel_only(args)
     return bench_gpu(args)
 
 

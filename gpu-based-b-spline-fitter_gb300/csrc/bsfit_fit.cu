@@ -92,9 +92,30 @@ struct Eval {
   static constexpr int NH = NV * (NV + 1) / 2;
 };
 
-template <int MODE, bool FISHER>
+// Row/column of item t of a row-major (rows x w) grid for a lane that starts at
+// t = lane and advances by 32: avoids a runtime integer division per item.
+struct Stride2D {
+  int r, c, dr, dc, w;
+  __device__ __forceinline__ Stride2D(int lane, int w_) : w(w_) {
+    r = lane / w;
+    c = lane - r * w;
+    dr = 32 / w;
+    dc = 32 - dr * w;
+  }
+  __device__ __forceinline__ void next() {
+    r += dr;
+    c += dc;
+    if (c >= w) {
+      c -= w;
+      ++r;
+    }
+  }
+};
+
+template <int MODE>
 __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int lane,
-                         const float* th, bool dup45, FPair& err_out, float (&jac)[ModeTraits<MODE>::NV],
+                         const float* th, bool dup45, bool FISHER, FPair& err_out,
+                         float (&jac)[ModeTraits<MODE>::NV],
                          float (&hes)[ModeTraits<MODE>::NV * (ModeTraits<MODE>::NV + 1) / 2]) {
   using TR = ModeTraits<MODE>;
   constexpr int D = TR::D;
@@ -167,8 +188,9 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
     const int nodes = wx * wy;
     if constexpr (D == 3) {
       const float* base = m.coeff + (int64_t)(kz - 1) * sz_;
-      for (int t = lane; t < nodes; t += 32) {
-        int xr = t / wy, yr = t - xr * wy;
+      Stride2D ix(lane, wy);
+      for (int t = lane; t < nodes; t += 32, ix.next()) {
+        const int xr = ix.r, yr = ix.c;
         const float* p = base + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
         float c0 = __ldg(p), c1 = __ldg(p + sz_), c2 = __ldg(p + 2 * sz_), c3 = __ldg(p + 3 * sz_);
         float v = c0 * bz0 + c1 * bz1 + c2 * bz2 + c3 * bz3;
@@ -182,8 +204,9 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
       const float dw[3] = {ww[4], ww[5], ww[6]};
       const int64_t sw_ = m.st[3];
       const float* base = m.coeff + (int64_t)(kz - 1) * sz_ + (int64_t)(kw - 1) * sw_;
-      for (int t = lane; t < nodes; t += 32) {
-        int xr = t / wy, yr = t - xr * wy;
+      Stride2D ix(lane, wy);
+      for (int t = lane; t < nodes; t += 32, ix.next()) {
+        const int xr = ix.r, yr = ix.c;
         const float* p = base + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
         float vz[4], dzv[4];
 #pragma unroll
@@ -210,8 +233,9 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
     const float dy0 = w[4], dy1 = w[5], dy2 = w[6];
     const int items = wx * s;
     const int gstride = wp * s;
-    for (int t = lane; t < items; t += 32) {
-      int xr = t / s, py = t - xr * s;
+    Stride2D ix(lane, s);
+    for (int t = lane; t < items; t += 32, ix.next()) {
+      const int xr = ix.r, py = ix.c;
       int oy = min(max(kys[py] - 1 - yb, 0), wy - 4);
       const float* a0 = A + xr * wp + oy;
       float v0 = a0[0], v1 = a0[1], v2 = a0[2], v3 = a0[3];
@@ -238,8 +262,9 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
     const float N = th[2], bg = th[3];
     const int gstride = wp * s;
     const int s2 = s * s;
-    for (int p = lane; p < s2; p += 32) {
-      int px = p / s, py = p - px * s;  // px = jj (X), py = ii (Y)
+    Stride2D ix(lane, s);
+    for (int p = lane; p < s2; p += 32, ix.next()) {
+      const int px = ix.r, py = ix.c;  // px = jj (X), py = ii (Y)
       int ox = min(max(kxs[px] - 1 - xb, 0), wx - 4);
       const float* g = G + ox * s + py;
       float g0 = g[0], g1 = g[s], g2 = g[2 * s], g3 = g[3 * s];
@@ -261,18 +286,21 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
       if (MODE == 7 && dup45) dudt[5] = dudt[4];
       const float model = bg + N * f;
       float d = data[p];
+      const float inv = __frcp_rn(model);
       if (!FISHER) {
-        // CPUmleFit_LM.cpp:2540-2559
+        // CPUmleFit_LM.cpp:2540-2559, with one reciprocal: d / m = d * (1 / m)
+        // and log(m / d) = -log(d / m).
         float term;
+        float dm = 0.0f;
         if (d > 0.0f) {
-          term = 2.0f * ((model - d) - d * logf(model / d));
+          dm = d * inv;
+          term = 2.0f * ((model - d) + d * logf(dm));
         } else {
           term = 2.0f * model;
-          d = 0.0f;
         }
         err.add(term);
-        const float t1 = 1.0f - d / model;
-        const float t2 = d / (model * model);
+        const float t1 = 1.0f - dm;
+        const float t2 = dm * inv;
 #pragma unroll
         for (int l = 0; l < NV; ++l) jac[l] = fmaf(t1, dudt[l], jac[l]);
         int k = 0;
@@ -284,7 +312,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
         }
       } else {
         // Fisher information and log-likelihood (CPUmleFit_LM.cpp:2730-2742).
-        const float im = 1.0f / model;
+        const float im = inv;
         int k = 0;
 #pragma unroll
         for (int l = 0; l < NV; ++l) {
@@ -420,9 +448,10 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     FPair tx{0.f, 0.f}, ty{0.f, 0.f}, ts{0.f, 0.f};
     float mx = 0.0f, mn = 10e10f;
     bool nan_seen = false;
-    for (int p = lane; p < s2; p += 32) {
+    Stride2D ix(lane, s);
+    for (int p = lane; p < s2; p += 32, ix.next()) {
       float d = data[p];
-      int jj = p / s, ii = p - jj * s;
+      const int jj = ix.r, ii = ix.c;
       tx.add(d * (float)ii);
       ty.add(d * (float)jj);
       ts.add(d);
@@ -458,7 +487,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     // evaluated in double as in the reference's expression.
     double n0 = ((double)mx - (double)mn) * 2.0 * (double)3.141592f * 1.5 * 1.5;
     th[2] = (float)((0.0 > n0) ? 0.0 : n0);
-    th[3] = (float)(((double)mn > 0.01) ? (double)mn : 0.01);
+    th[3] = (mn > 0.01f) ? mn : 0.01f;
     if (MODE == 6) {
       th[4] = (float)a.m.n[2] / 2.0f;
     } else if (MODE == 7) {
@@ -495,10 +524,28 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   float jac[NV], hes[NH];
   int turn = 1;
 
-  evaluate<MODE, false>(a, L, ws, lane, th, MODE == 7, err, jac, hes);
-
+  // One evaluation call site for the initial pass, every accepted step and the
+  // final CRLB pass (keeps the kernel's instruction footprint small).
   int kk = 0;
-  for (kk = 0; kk < a.iterations; kk++) {
+  bool need_eval = true, first = true, fisher = false;
+  FPair ll{0.0f, 0.0f};
+  for (;;) {
+    if (need_eval) {
+      FPair e;
+      evaluate<MODE>(a, L, ws, lane, th, first && MODE == 7, fisher, e, jac, hes);
+      first = false;
+      need_eval = false;
+      if (fisher) {
+        ll = e;
+        break;
+      }
+      err = e;
+    }
+    if (kk >= a.iterations) {
+      fisher = true;
+      need_eval = true;
+      continue;
+    }
     float* rec = (a.trace && kk < a.trace_max && lane == 0)
                      ? a.trace + (roi * (int64_t)a.trace_max + kk) * TRACE_REC
                      : nullptr;
@@ -516,11 +563,15 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
       }
       if (rel < 1e-6f) {
         if (rec) rec[4] = 1.0f;
-        break;
+        fisher = true;
+        need_eval = true;
+        continue;
       }
     }
     const float e_new = err.hi + err.lo, e_old = oerr.hi + oerr.lo;
-    if ((double)e_new > 1.5 * (double)e_old) {
+    // newErr > 1.5 * oldErr, evaluated in double by the reference: the FMA
+    // forms 1.5 * oldErr - newErr with one rounding, which keeps its sign.
+    if (fmaf(1.5f, e_old, -e_new) < 0.0f) {
 #pragma unroll
       for (int i = 0; i < NV; i++) {
         sign[i] = osign[i];
@@ -629,24 +680,26 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
         th[l] = th[l] - upd[l] / (1.0f + fabsf(upd[l] / clampv[l]));
       }
       th[2] = (th[2] > 1.0f) ? th[2] : 1.0f;
-      th[3] = ((double)th[3] > 0.01) ? th[3] : 0.01f;
+      // max(bg, 0.01) in double: no float lies strictly between 0.01f and 0.01,
+      // so the float comparison selects the same branch.
+      th[3] = (th[3] > 0.01f) ? th[3] : 0.01f;
       th[4] = (th[4] > 0.0f) ? th[4] : 0.0f;
       if (MODE == 6) {
         float zmax = (float)(a.m.n[2] - 4);
         th[4] = (th[4] < zmax) ? th[4] : zmax;
       } else {
-        double zmax = (double)a.m.n[2] - 0.5;
-        th[4] = ((double)th[4] < zmax) ? th[4] : (float)zmax;
+        const float zmax = (float)a.m.n[2] - 0.5f;  // exact: n - 0.5 is a float
+        th[4] = (th[4] < zmax) ? th[4] : zmax;
         th[5] = (th[5] > 0.0f) ? th[5] : 0.0f;
-        double wmax = (double)a.m.n[3] - 0.5;
-        th[5] = ((double)th[5] < wmax) ? th[5] : (float)wmax;
+        const float wmax = (float)a.m.n[3] - 0.5f;
+        th[5] = (th[5] < wmax) ? th[5] : wmax;
       }
-      evaluate<MODE, false>(a, L, ws, lane, th, false, err, jac, hes);
+      need_eval = true;
     } else {
       lambda = 10.0f * lambda;
     }
     if (rec) {
-      const float e_n = err.hi + err.lo;
+      const float e_n = 0.0f;  // deviance after the step: next record's [2]
       rec[4] = (e_new > 1.5f * e_old ? 2.0f : 0.0f) + (e_new < e_old ? 4.0f : 0.0f) + (ok ? 8.0f : 0.0f);
       rec[5] = lambda;
 #pragma unroll
@@ -655,12 +708,11 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
       for (int i = 0; i < NV; ++i) rec[14 + i] = th[i];
       rec[22] = e_n;
     }
+    ++kk;
   }
 
-  // CRLB and log-likelihood at the final theta.
-  FPair ll;
-  float fj[NV], fm[NH];
-  evaluate<MODE, true>(a, L, ws, lane, th, false, ll, fj, fm);
+  // CRLB and log-likelihood at the final theta (the Fisher pass above).
+  float* fm = hes;
   double M[NV * NV], diag[NV];
 #pragma unroll
   for (int l = 0; l < NV; ++l)
@@ -720,10 +772,7 @@ __global__ void __launch_bounds__(128) eval_kernel(FitArgs a, const float* theta
     for (int i = 0; i < NV; ++i) th[i] = theta[i * a.nfits + roi];
     FPair e;
     float jac[NV], hes[NH];
-    if (fisher)
-      evaluate<MODE, true>(a, L, ws, lane, th, false, e, jac, hes);
-    else
-      evaluate<MODE, false>(a, L, ws, lane, th, false, e, jac, hes);
+    evaluate<MODE>(a, L, ws, lane, th, false, fisher != 0, e, jac, hes);
     if (lane == 0) {
       float* o = out + roi * (1 + NV + NH);
       o[0] = e.hi + e.lo;

@@ -262,7 +262,7 @@ def bench_gpu(args):
         return 0
     cpu_n, cpu_t = run_cpu(groups, os.cpu_count() or 1, 0.016)
     # DRAM traffic of the fitter per step: the ncu capture of the 13 px case
-    # (profiles/fit_kernel_3d13.md) measured bytes per ROI against the
+    # (summarised under profiles/) measured bytes per ROI against the
     # algorithmic 4 s^2 + 48 B; the step's traffic scales that ratio by each
     # size group's algorithmic bytes (traffic grows with the pixels read).
     traffic = None

@@ -74,7 +74,7 @@ def _erf(x):
     try:
         from scipy.special import erf
         return erf(x)
-    except ImportError:  # pragma: no cover - the GPU machine has scipy
+    except ImportError:  # pragma: no cover - scipy is normally present
         return np.vectorize(math.erf)(x)
 
 

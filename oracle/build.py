@@ -1,10 +1,10 @@
 """Build recipe for the oracle (test infrastructure only).
 
 - ``liboracle.so``: the CPU restatement in ``bsfit_oracle.cpp``, built on
-  every machine (this container and the GPU machine).
+  every machine that runs the tests, the smoke check or the benchmark.
 - ``_ref/libref_f32.so`` / ``_ref/libref_f64.so``: the reference's own CPU
   fitter compiled from its sources by ``build_ref.sh``, only where the reference
-  sources exist (not on the GPU machine).
+  sources exist; elsewhere the restatement alone is the oracle.
 """
 import os
 import subprocess

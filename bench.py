@@ -258,6 +258,29 @@ def bench_gpu(args):
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_value = n_step * world / e2e_s
 
+    # The metric's per-model figures: 3D 13 px from the per-size timing above,
+    # 5D 17 px (fit type 8, 60 iterations) on its own synthetic workload.
+    fits_3d13 = None
+    for g, t in zip(groups, per_launch):
+        if g.roi_size == 13:
+            fits_3d13 = len(g.rois) / (t * 1e-3)
+    fits_5d17 = None
+    if not args.no_5d:
+        from bsfit import workloads as W
+        w5 = W.workload_5d(args.rois_5d, s=17, stream=7)
+        m5 = bsfit.Model(8, w5.coeff, coeff3=w5.coeff3, init_p=w5.init_p)
+        r5 = torch.from_numpy(w5.rois).to(dev)
+        o5 = (torch.empty((9, len(w5.rois)), device=dev), torch.empty((8, len(w5.rois)), device=dev),
+              torch.empty((len(w5.rois),), device=dev))
+        with torch.cuda.stream(stream):
+            m5.fit_torch(r5, w5.iterations, out=o5, stream=stream)
+            a5, b5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a5.record(stream)
+            for _ in range(2):
+                m5.fit_torch(r5, w5.iterations, out=o5, stream=stream)
+            b5.record(stream)
+        stream.synchronize()
+        fits_5d17 = len(w5.rois) / (a5.elapsed_time(b5) / 2 * 1e-3)
     if rank != 0:
         return 0
     cpu_n, cpu_t = run_cpu(groups, os.cpu_count() or 1, 0.016)
@@ -295,6 +318,8 @@ def bench_gpu(args):
                          "kind": "port",
                          "sample": f"{cpu_n} ROIs (1.6% of each size group), FP32 oracle port of "
                                    f"the reference CPU fitter, OpenMP over ROIs"},
+        "fits_per_s": {"3d_13px": fits_3d13, "5d_17px": fits_5d17,
+                       "5d_workload": f"{args.rois_5d} ROIs 17x17, fit type 8, 60 iterations"},
         "clocks": clk.summary(),
         "gpu_launches": args.steps * len(groups),
     }
@@ -312,6 +337,8 @@ def main():
                     help="profiling case: only the fit launches of --rois ROIs of --sizes")
     ap.add_argument("--rois", type=int, default=N_ROIS)
     ap.add_argument("--sizes", type=int, nargs="+", default=list(SIZES))
+    ap.add_argument("--rois-5d", type=int, default=50000, help="ROIs of the 5D 17 px figure")
+    ap.add_argument("--no-5d", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)

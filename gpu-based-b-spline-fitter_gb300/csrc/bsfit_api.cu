@@ -129,12 +129,12 @@ int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
   if (st) return st;
   if (fittype == 7 && (!init_p || init_p_numel < 2)) return BSFIT_E_INIT_P;
   if (fittype == 8) {
-    if (init_p && init_p_numel < 4) return BSFIT_E_INIT_P;
+    // The reference leaves g2 uninitialised without initP (CPUmleFit_LM.cpp:3246-3256).
+    if (!init_p || init_p_numel < 4) return BSFIT_E_INIT_P;
     if (!coeff3 || !coeff3_dims || coeff3_ndim != 3) return BSFIT_E_WRONG_DATA_TYPE;
     for (int i = 0; i < 3; ++i)
       if (coeff3_dims[i] != coeff_dims[i]) return BSFIT_E_COEFF_SIZE;
   }
-  if (fittype == 8) return BSFIT_E_UNSUPPORTED_FITTYPE;  // kernel not built yet
   bsfit_model_s* m = new (std::nothrow) bsfit_model_s;
   if (!m) return BSFIT_E_NOT_ENOUGH_MEMORY;
   fill_model(m->dev, fittype, coeff_dims, init_p, init_p_numel);

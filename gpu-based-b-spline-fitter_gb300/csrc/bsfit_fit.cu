@@ -56,6 +56,19 @@ struct ModeTraits<7> {
   static constexpr int NG = 4;  // value, d/dY, d/dz, d/dw
 };
 
+template <>
+struct ModeTraits<8> {
+  static constexpr int D = 5;
+  static constexpr int NV = 8;
+  // value, d/dz, d/dw, d/du of the 5D spline, the two correction maps of the
+  // reference's 5D derivative (z term 27, u term 16), value and d/dz of the 3D
+  // spline
+  static constexpr int NA = 8;
+  // value, d/dY, d/dz, d/dw, d/du, z correction, u correction (5D); value,
+  // d/dY, d/dz (3D)
+  static constexpr int NG = 10;
+};
+
 // Per-warp shared-memory layout (floats). WP = s + 4 bounds the knot window
 // along each lateral axis.
 struct WarpLayout {
@@ -73,8 +86,8 @@ __host__ __device__ inline WarpLayout make_layout(int mode, int s) {
   L.s = s;
   L.s2p = (s * s + 3) & ~3;
   L.wp = s + 4;
-  L.na = mode == 6 ? 2 : 3;
-  L.ng = mode == 6 ? 3 : 4;
+  L.na = mode == 6 ? 2 : mode == 7 ? 3 : 8;
+  L.ng = mode == 6 ? 3 : mode == 7 ? 4 : 10;
   return L;
 }
 
@@ -139,6 +152,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
   const float off = (float)(m.n[1] - s) / 2.0f;
   const float zc = th[4];
   const float wc = (D >= 4) ? th[5] : 0.0f;
+  const float uc = (D >= 5) ? th[6] : 0.0f;
 
   for (int j = lane; j < s; j += 32) {
     kxs[j] = knot_index((xc + (float)j) + off, m.n[1]);
@@ -146,14 +160,16 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
   }
   // Fractional parts (Y, X, Z, W) and the 1-D weights, one per lane.
   {
-    float fr[4];
+    float fr[5];
     fr[0] = yc - floorf(yc);
     fr[1] = xc - floorf(xc);
     fr[2] = zc - floorf(zc);
     fr[3] = wc - floorf(wc);
-    if (lane < 7 * D) {
-      int ax = lane / 7;
-      w[ax * 8 + (lane % 7)] = axis_weight(fr[ax], lane % 7);
+    fr[4] = uc - floorf(uc);
+    // 7 weights per axis: 35 for the 5D model, more than one per lane.
+    for (int k = lane; k < 7 * D; k += 32) {
+      const int ax = k / 7;
+      w[ax * 8 + (k - ax * 7)] = axis_weight(fr[ax], k - ax * 7);
     }
   }
   __syncwarp();
@@ -178,6 +194,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
   const int yb = kymin - 1, wy = min(kymax - kymin + 4, wp);
   const int kz = knot_index(zc, m.n[2]);
   const int kw = (D >= 4) ? knot_index(wc, m.n[3]) : 0;
+  const int ku = (D >= 5) ? knot_index(uc, m.n[4]) : 0;
 
   // (A) Non-lateral contraction at every lateral node of the window.
   {
@@ -198,7 +215,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
         A[xr * wp + yr] = v;
         A[wp * wp + xr * wp + yr] = dz;
       }
-    } else {
+    } else if constexpr (D == 4) {
       const float* ww = w + 3 * 8;
       const float bw[4] = {ww[0], ww[1], ww[2], ww[3]};
       const float dw[3] = {ww[4], ww[5], ww[6]};
@@ -223,6 +240,104 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
         A[wp * wp + xr * wp + yr] = dz;
         A[2 * wp * wp + xr * wp + yr] = dwv;
       }
+    } else {
+      // 5D (z, w, u) for the mixture's 5D part, plus its 3D part (z only, on
+      // coeff3 with the same lateral and z knots).
+      const float* ww = w + 3 * 8;
+      const float* wu = w + 4 * 8;
+      const float bw[4] = {ww[0], ww[1], ww[2], ww[3]};
+      const float dw[3] = {ww[4], ww[5], ww[6]};
+      const float bu[4] = {wu[0], wu[1], wu[2], wu[3]};
+      const float du[3] = {wu[4], wu[5], wu[6]};
+      // Correction weights of the reference's z-derivative term 27 (reads
+      // delta_dfz[32 n + 271], CPUsplineLib.cpp:313): per (lvZ, lvW, lvU) the
+      // non-lateral factor R' of the weight actually read minus the factor R of
+      // the intended weight dBz1(lvZ) Bw2(lvW) Bu2(lvU). For v = (lvW-1) +
+      // 2 (lvU-1) < 3 the read weight is delta_dfz of block n + 8, i.e.
+      // dBz2(lvZ) Bw2(lvW') Bu1(lvU') with v' = v + 1; for v = 3 it is the
+      // W-derivative weight of block n - 24: Bz2(lvZ) dBw2(1) Bu1(1). The
+      // lateral factor By2 Bx2 is the same in both.
+      // Local node index per axis: offset + 1 (offsets -1..+2).
+      // side 1, lv -> offset 1 - lv; side 2, lv -> offset lv.
+      float R[2][2][2];  // [lvZ-1][lvW-1][lvU-1]
+#pragma unroll
+      for (int lz = 1; lz <= 2; ++lz)
+#pragma unroll
+        for (int lw = 1; lw <= 2; ++lw)
+#pragma unroll
+          for (int lu = 1; lu <= 2; ++lu) {
+            const int v = (lw - 1) + 2 * (lu - 1);
+            const float dBz1 = (lz == 1) ? dz1 : dz0;   // side 1 derivative, offsets 0 / -1
+            const float dBz2 = (lz == 1) ? dz2 : 0.0f;  // side 2 derivative, offsets +1 / +2
+            const float Bz2 = (lz == 1) ? bz2 : bz3;
+            float rp;
+            if (v < 3) {
+              const int vp = v + 1, lwp = (vp & 1) + 1, lup = (vp >> 1) + 1;
+              rp = dBz2 * (lwp == 1 ? bw[2] : bw[3]) * (lup == 1 ? bu[1] : bu[0]);
+            } else {
+              rp = Bz2 * dw[2] * bu[1];
+            }
+            R[lz - 1][lw - 1][lu - 1] = rp - dBz1 * (lw == 1 ? bw[2] : bw[3]) * (lu == 1 ? bu[2] : bu[3]);
+          }
+      const int64_t sw_ = m.st[3], su_ = m.st[4];
+      const float* base = m.coeff + (int64_t)(kz - 1) * sz_ + (int64_t)(kw - 1) * sw_ +
+                          (int64_t)(ku - 1) * su_;
+      const float* base3 = m.coeff3 + (int64_t)(kz - 1) * sz_;
+      Stride2D ix(lane, wy);
+      const int ws2 = wp * wp;
+      for (int t = lane; t < nodes; t += 32, ix.next()) {
+        const int xr = ix.r, yr = ix.c;
+        const int64_t lat = (int64_t)(xb + xr) * m.st[1] + (yb + yr);
+        const float* p = base + lat;
+        float vz[4][4], dzz[4][4];   // [u][w]
+        float qz = 0.0f;             // z-term-27 correction
+        float sq[4][2];              // [u][w in {0,1}]: sum over z in {0,1} of Bz * C
+#pragma unroll
+        for (int iu = 0; iu < 4; ++iu)
+#pragma unroll
+          for (int iw = 0; iw < 4; ++iw) {
+            const float* q = p + iu * su_ + iw * sw_;
+            float c0 = __ldg(q), c1 = __ldg(q + sz_), c2 = __ldg(q + 2 * sz_), c3 = __ldg(q + 3 * sz_);
+            vz[iu][iw] = c0 * bz0 + c1 * bz1 + c2 * bz2 + c3 * bz3;
+            dzz[iu][iw] = (c1 - c0) * dz0 + (c2 - c1) * dz1 + (c3 - c2) * dz2;
+            if (iw >= 2 && iu >= 2) {
+              // lvW = iw - 1, lvU = iu - 1; Z nodes 1 - lvZ: local 1 (lvZ 1), 0 (lvZ 2)
+              qz += (c2 - c1) * R[0][iw - 2][iu - 2] + (c1 - c0) * R[1][iw - 2][iu - 2];
+            }
+            if (iw <= 1) sq[iu][iw] = c0 * bz0 + c1 * bz1;
+          }
+        float vw[4], dzw[4], dww[4];
+#pragma unroll
+        for (int iu = 0; iu < 4; ++iu) {
+          vw[iu] = vz[iu][0] * bw[0] + vz[iu][1] * bw[1] + vz[iu][2] * bw[2] + vz[iu][3] * bw[3];
+          dzw[iu] = dzz[iu][0] * bw[0] + dzz[iu][1] * bw[1] + dzz[iu][2] * bw[2] + dzz[iu][3] * bw[3];
+          dww[iu] = (vz[iu][1] - vz[iu][0]) * dw[0] + (vz[iu][2] - vz[iu][1]) * dw[1] +
+                    (vz[iu][3] - vz[iu][2]) * dw[2];
+        }
+        const float v = vw[0] * bu[0] + vw[1] * bu[1] + vw[2] * bu[2] + vw[3] * bu[3];
+        const float dzv = dzw[0] * bu[0] + dzw[1] * bu[1] + dzw[2] * bu[2] + dzw[3] * bu[3];
+        const float dwv = dww[0] * bu[0] + dww[1] * bu[1] + dww[2] * bu[2] + dww[3] * bu[3];
+        const float duv = (vw[1] - vw[0]) * du[0] + (vw[2] - vw[1]) * du[1] + (vw[3] - vw[2]) * du[2];
+        // u-term-16 correction (CPUsplineLib.cpp:420-421): the term differences
+        // the U node at offset 0 instead of +1 with weight
+        // By1 Bx1 Bz1 Bw1 dBu2(1); lateral side 1 and z, w at offsets -1 / 0.
+        float qu = 0.0f;
+#pragma unroll
+        for (int iw = 0; iw < 2; ++iw)
+          qu += bw[iw] * ((sq[2][iw] - sq[1][iw]) - (sq[3][iw] - sq[2][iw]));
+        qu *= du[2];
+        const float* p3 = base3 + lat;
+        float e0 = __ldg(p3), e1 = __ldg(p3 + sz_), e2 = __ldg(p3 + 2 * sz_), e3 = __ldg(p3 + 3 * sz_);
+        const int o = xr * wp + yr;
+        A[o] = v;
+        A[ws2 + o] = dzv;
+        A[2 * ws2 + o] = dwv;
+        A[3 * ws2 + o] = duv;
+        A[4 * ws2 + o] = qz;
+        A[5 * ws2 + o] = qu;
+        A[6 * ws2 + o] = e0 * bz0 + e1 * bz1 + e2 * bz2 + e3 * bz3;
+        A[7 * ws2 + o] = (e1 - e0) * dz0 + (e2 - e1) * dz1 + (e3 - e2) * dz2;
+      }
     }
   }
   __syncwarp();
@@ -241,10 +356,30 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
       float v0 = a0[0], v1 = a0[1], v2 = a0[2], v3 = a0[3];
       G[xr * s + py] = v0 * by0 + v1 * by1 + v2 * by2 + v3 * by3;
       G[gstride + xr * s + py] = (v1 - v0) * dy0 + (v2 - v1) * dy1 + (v3 - v2) * dy2;
+      if constexpr (MODE != 8) {
 #pragma unroll
-      for (int c = 1; c < TR::NA; ++c) {
-        const float* ac = a0 + c * wp * wp;
-        G[(c + 1) * gstride + xr * s + py] = ac[0] * by0 + ac[1] * by1 + ac[2] * by2 + ac[3] * by3;
+        for (int c = 1; c < TR::NA; ++c) {
+          const float* ac = a0 + c * wp * wp;
+          G[(c + 1) * gstride + xr * s + py] = ac[0] * by0 + ac[1] * by1 + ac[2] * by2 + ac[3] * by3;
+        }
+      } else {
+        const int ws2 = wp * wp;
+        const int o = xr * s + py;
+#pragma unroll
+        for (int c = 1; c <= 3; ++c) {  // d/dz, d/dw, d/du of the 5D spline
+          const float* ac = a0 + c * ws2;
+          G[(c + 1) * gstride + o] = ac[0] * by0 + ac[1] * by1 + ac[2] * by2 + ac[3] * by3;
+        }
+        const float* qz = a0 + 4 * ws2;  // lateral side 2: offsets +1, +2
+        G[5 * gstride + o] = qz[2] * by2 + qz[3] * by3;
+        const float* qu = a0 + 5 * ws2;  // lateral side 1: offsets -1, 0
+        G[6 * gstride + o] = qu[0] * by0 + qu[1] * by1;
+        const float* b3 = a0 + 6 * ws2;  // 3D spline value
+        float u0 = b3[0], u1 = b3[1], u2 = b3[2], u3 = b3[3];
+        G[7 * gstride + o] = u0 * by0 + u1 * by1 + u2 * by2 + u3 * by3;
+        G[8 * gstride + o] = (u1 - u0) * dy0 + (u2 - u1) * dy1 + (u3 - u2) * dy2;
+        const float* z3 = a0 + 7 * ws2;
+        G[9 * gstride + o] = z3[0] * by0 + z3[1] * by1 + z3[2] * by2 + z3[3] * by3;
       }
     }
   }
@@ -277,14 +412,51 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
       dudt[1] = -N * dY;
       dudt[2] = f;
       dudt[3] = 1.0f;
+      float model;
+      if constexpr (MODE != 8) {
 #pragma unroll
-      for (int c = 1; c < TR::NA; ++c) {
-        const float* gc = g + (c + 1) * gstride;
-        float dc = gc[0] * bx0 + gc[s] * bx1 + gc[2 * s] * bx2 + gc[3 * s] * bx3;
-        dudt[3 + c] = N * dc;
+        for (int c = 1; c < TR::NA; ++c) {
+          const float* gc = g + (c + 1) * gstride;
+          float dc = gc[0] * bx0 + gc[s] * bx1 + gc[2 * s] * bx2 + gc[3 * s] * bx3;
+          dudt[3 + c] = N * dc;
+        }
+        if (MODE == 7 && dup45) dudt[5] = dudt[4];
+        model = bg + N * f;
+      } else {
+        // 5D derivatives with the reference's two term corrections
+        const float* gz = g + 2 * gstride;
+        const float* gw = g + 3 * gstride;
+        const float* gu = g + 4 * gstride;
+        const float* gqz = g + 5 * gstride;
+        const float* gqu = g + 6 * gstride;
+        float dZ = gz[0] * bx0 + gz[s] * bx1 + gz[2 * s] * bx2 + gz[3 * s] * bx3 +
+                   (gqz[2 * s] * bx2 + gqz[3 * s] * bx3);
+        float dW = gw[0] * bx0 + gw[s] * bx1 + gw[2 * s] * bx2 + gw[3 * s] * bx3;
+        float dU = gu[0] * bx0 + gu[s] * bx1 + gu[2 * s] * bx2 + gu[3 * s] * bx3 +
+                   (gqu[0] * bx0 + gqu[s] * bx1);
+        // 3D spline
+        const float* h = g + 7 * gstride;
+        float h0 = h[0], h1 = h[s], h2 = h[2 * s], h3 = h[3 * s];
+        float f3 = h0 * bx0 + h1 * bx1 + h2 * bx2 + h3 * bx3;
+        float dX3 = (h1 - h0) * dx0 + (h2 - h1) * dx1 + (h3 - h2) * dx2;
+        const float* hy = g + 8 * gstride;
+        float dY3 = hy[0] * bx0 + hy[s] * bx1 + hy[2 * s] * bx2 + hy[3 * s] * bx3;
+        const float* hz = g + 9 * gstride;
+        float dZ3 = hz[0] * bx0 + hz[s] * bx1 + hz[2 * s] * bx2 + hz[3 * s] * bx3;
+        // mixture (CPUmleFit_LM.cpp:3311-3322)
+        const float g2 = th[7], h2m = 1.0f - g2;
+        const float m5 = bg + N * f, m3 = bg + N * f3;
+        dudt[0] = dudt[0] * g2 + h2m * (-N * dX3);
+        dudt[1] = dudt[1] * g2 + h2m * (-N * dY3);
+        dudt[2] = f * g2 + h2m * f3;
+        dudt[3] = g2 + h2m;
+        dudt[4] = (N * dZ) * g2 + h2m * (N * dZ3);
+        dudt[5] = N * dW;
+        dudt[6] = N * dU;
+        // m5 - m3 = N (f5 - f3): formed without the background, which cancels
+        dudt[NV - 1] = N * (f - f3);
+        model = m3 * h2m + m5 * g2;
       }
-      if (MODE == 7 && dup45) dudt[5] = dudt[4];
-      const float model = bg + N * f;
       float d = data[p];
       const float inv = __frcp_rn(model);
       if (!FISHER) {
@@ -498,6 +670,10 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
         th[4] = (float)a.m.n[2] / 2.0f;
         th[5] = (float)a.m.n[3] / 2.0f;
       }
+    } else {
+      // (z, w, u, g2) from initP, shared by all ROIs (CPUmleFit_LM.cpp:3246-3256)
+#pragma unroll
+      for (int i = 4; i < NV; ++i) th[i % NV] = a.m.init_p[(i - 4) & 3];
     }
   }
 
@@ -513,12 +689,21 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     const float c[5] = {2.0f, 2.0f, 10000.0f, 20.0f, 20.0f};
 #pragma unroll
     for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = c[i % 5], fade[i] = 0.5f;
-  } else {
+  } else if (MODE == 7) {
     const float c[6] = {1.0f, 1.0f, 10000.0f, 20.0f, 2.0f, 0.00001f};
     const float fd[6] = {0.5f, 0.5f, 0.4f, 0.5f, 0.7f, 0.8f};
 #pragma unroll
     for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = c[i % 6], fade[i] = fd[i % 6];
+  } else {
+    // CPUmleFit_LM.cpp:3191-3193
+    const float c[8] = {1.0f, 1.0f, 10000.0f, 20.0f, 2.0f, 2.0f, 2.0f, 0.1f};
+#pragma unroll
+    for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = c[i % 8], fade[i] = 0.5f;
   }
+  float sum_update = 1e10f;
+  // Parameters of the last evaluation: fit type 8's CRLB pass reuses its
+  // positions, weights and g2 (CPUmleFit_LM.cpp:3568-3584).
+  float th_eval[NV];
   float lambda = 1.0f, olambda = 1.0f;
   FPair err{1e12f, 0.0f}, oerr{1e13f, 0.0f};
   float jac[NV], hes[NH];
@@ -532,7 +717,13 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   for (;;) {
     if (need_eval) {
       FPair e;
-      evaluate<MODE>(a, L, ws, lane, th, first && MODE == 7, fisher, e, jac, hes);
+      float the[NV];
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        if (!fisher) th_eval[i] = th[i];
+        the[i] = (MODE == 8 && i != 2 && i != 3) ? th_eval[i] : th[i];
+      }
+      evaluate<MODE>(a, L, ws, lane, the, first && MODE == 7, fisher, e, jac, hes);
       first = false;
       need_eval = false;
       if (fisher) {
@@ -561,7 +752,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
         rec[3] = oerr.hi + oerr.lo;
         rec[4] = 0.0f;
       }
-      if (rel < 1e-6f) {
+      if (rel < 1e-6f || (MODE == 8 && sum_update < 1e-5f)) {  // :3355
         if (rec) rec[4] = 1.0f;
         fisher = true;
         need_eval = true;
@@ -670,6 +861,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
           oclamp[4] = 2.0f;
         }
       }
+      if (MODE == 8) sum_update = 0.0f;
 #pragma unroll
       for (int l = 0; l < NV; l++) {
         if (sign[l] != 0.0f) {
@@ -677,7 +869,18 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
             clampv[l] = clampv[l] * fade[l];
         }
         sign[l] = (upd[l] > 0.0f) ? 1.0f : -1.0f;
-        th[l] = th[l] - upd[l] / (1.0f + fabsf(upd[l] / clampv[l]));
+        const float step = upd[l] / (1.0f + fabsf(upd[l] / clampv[l]));
+        th[l] = th[l] - step;
+        if (MODE == 8) sum_update += fabsf(step);
+      }
+      if (MODE == 8) {
+        // x, y within (s-1)/2 +- s/4 (exact in float for s <= 51), CPUmleFit_LM.cpp:3421-3424
+        const float lo = (float)(s - 1) / 2.0f - (float)s / 4.0f;
+        const float hi = (float)(s - 1) / 2.0f + (float)s / 4.0f;
+        th[0] = (th[0] > lo) ? th[0] : lo;
+        th[0] = (th[0] < hi) ? th[0] : hi;
+        th[1] = (th[1] > lo) ? th[1] : lo;
+        th[1] = (th[1] < hi) ? th[1] : hi;
       }
       th[2] = (th[2] > 1.0f) ? th[2] : 1.0f;
       // max(bg, 0.01) in double: no float lies strictly between 0.01f and 0.01,
@@ -687,12 +890,26 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
       if (MODE == 6) {
         float zmax = (float)(a.m.n[2] - 4);
         th[4] = (th[4] < zmax) ? th[4] : zmax;
-      } else {
+      } else if (MODE == 7) {
         const float zmax = (float)a.m.n[2] - 0.5f;  // exact: n - 0.5 is a float
         th[4] = (th[4] < zmax) ? th[4] : zmax;
         th[5] = (th[5] > 0.0f) ? th[5] : 0.0f;
         const float wmax = (float)a.m.n[3] - 0.5f;
         th[5] = (th[5] < wmax) ? th[5] : wmax;
+      } else {
+        const float zmax = (float)a.m.n[2] - 0.5f;
+        th[4] = (th[4] < zmax) ? th[4] : zmax;
+        // periodic azimuth (CPUmleFit_LM.cpp:3436-3443): period nW - 2
+        const int nw = a.m.n[3];
+        if (th[5] <= 1.0f)
+          th[5] = (float)(nw - 2) + th[5];
+        else if (th[5] > (float)(nw - 1))
+          th[5] = (2.0f + th[5]) - (float)nw;
+        th[6] = (th[6] > 1.0f) ? th[6] : 1.0f;
+        const float umax = (float)a.m.n[4] - 0.5f;
+        th[6] = (th[6] < umax) ? th[6] : umax;
+        th[7 % NV] = (th[7 % NV] < 1.0f) ? th[7 % NV] : 1.0f;
+        th[7 % NV] = (th[7 % NV] > 0.0f) ? th[7 % NV] : 0.0f;
       }
       need_eval = true;
     } else {
@@ -796,6 +1013,7 @@ cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fi
   void (*kern)(FitArgs, const float*, float*, int) = nullptr;
   if (mode == 6) kern = eval_kernel<6>;
   else if (mode == 7) kern = eval_kernel<7>;
+  else if (mode == 8) kern = eval_kernel<8>;
   else return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
@@ -860,19 +1078,31 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
   }
   const int mode = a.m.fittype;
   const int per_warp = warp_smem_floats(mode, a.s) * 4;
-  int wpb = 4;
-  while (wpb > 1 && per_warp * wpb > 200 * 1024) wpb >>= 1;
-  const int smem = per_warp * wpb;
   void (*kern)(FitArgs) = nullptr;
   if (mode == 6) kern = fit_kernel<6>;
   else if (mode == 7) kern = fit_kernel<7>;
+  else if (mode == 8) kern = fit_kernel<8>;
   else return cudaErrorInvalidValue;
+  // Warps per block: the choice among 4, 2, 1 that keeps the most warps
+  // resident per SM (shared memory per warp grows with s and the model).
+  int wpb = 4, blocks_per_sm = 0, best = -1;
+  for (int cand = 4; cand >= 1; cand >>= 1) {
+    const int sm = per_warp * cand;
+    if (sm > 220 * 1024) continue;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
+      continue;
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * cand, sm) != cudaSuccess) continue;
+    if (b * cand > best) {
+      best = b * cand;
+      wpb = cand;
+      blocks_per_sm = b;
+    }
+  }
+  if (best <= 0) return cudaErrorInvalidConfiguration;
+  const int smem = per_warp * wpb;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  int blocks_per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, 32 * wpb, smem);
-  if (e != cudaSuccess) return e;
-  if (blocks_per_sm < 1) blocks_per_sm = 1;
   int64_t need = (a.nfits + wpb - 1) / wpb;
   int64_t grid = (int64_t)g_num_sms * blocks_per_sm;
   if (need < grid) grid = need;

@@ -49,7 +49,8 @@ typedef enum bsfit_status {
   /* coefficient array too small (< 5 along an axis), wrong rank, or lateral
    * sizes unequal (the reference indexes past the array there) */
   BSFIT_E_COEFF_SIZE = 9,
-  /* initP missing or too short for fit type 7 (the reference dereferences it) */
+  /* initP missing or too short for fit types 7 and 8 (the reference
+   * dereferences it, or leaves g2 uninitialised) */
   BSFIT_E_INIT_P = 10,
   /* invalid handle or argument of the device-level API */
   BSFIT_E_INVALID = 11,
@@ -79,7 +80,8 @@ const char* bsfit_version(void);
  * silent: 0 prints the reference's summary lines to stdout.
  * init_p: fit type 7: (z, w), both taken from init_p when init_p[0] != 0,
  *   else mid-grid (CPUmleFit_LM.cpp:2841-2850); fit type 8: (z, w, u, g2),
- *   NULL for mid-grid z, w, u (CPUmleFit_LM.cpp:3246-3256); ignored for 6.
+ *   required (without it the reference leaves g2 uninitialised,
+ *   CPUmleFit_LM.cpp:3246-3256); ignored for 6.
  * coeff3: fit type 8 only, the 3D coefficients (same Y, X, Z sizes).
  * P, CRLB, LL: caller-allocated host outputs.
  */

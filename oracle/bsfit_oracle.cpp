@@ -1011,3 +1011,29 @@ void oracle_trace_f64(int fittype, const double* data, const double* coeff, cons
   }
 }
 }  // extern "C"
+
+namespace {
+// Fit type 8 evaluation at given theta (the mixture model of Model53D).
+void eval8(const double* rois, const double* coeff5, const double* coeff3, const int* dims, int sz,
+           int nfits, const double* theta, int fisher, double* out) {
+  Model53D<double>* m = new Model53D<double>;
+  m->coeff5 = coeff5;
+  m->coeff3 = coeff3;
+  m->n[0] = dims[1] - 3;
+  m->n[1] = dims[0] - 3;
+  m->n[2] = dims[2] - 3;
+  m->n[3] = dims[3] - 3;
+  m->n[4] = dims[4] - 3;
+  eval_entry<double, Model53D<double>>(*m, rois, sz, nfits, theta, fisher, out);
+  delete m;
+}
+}  // namespace
+
+extern "C" {
+void oracle_eval8_f64(const double* rois, const double* coeff5, const double* coeff3, int cx,
+                      int cy, int cz, int cw, int cu, int sz, int nfits, const double* theta,
+                      int fisher, double* out) {
+  int dims[5] = {cx, cy, cz, cw, cu};
+  eval8(rois, coeff5, coeff3, dims, sz, nfits, theta, fisher, out);
+}
+}  // extern "C"

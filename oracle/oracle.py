@@ -112,7 +112,7 @@ class ReferenceOracle(_Base):
         return self._libs[np.float32].ref_eval_bspline_f32(x, deg)
 
 
-def _eval_entry(self, rois, fittype, coeff, theta, fisher=False):
+def _eval_entry(self, rois, fittype, coeff, theta, fisher=False, coeff3=None):
     """One evaluation per ROI at theta ((N, NV) array): returns (N, 1+NV+NH)
     float64 rows [value, gradient, packed upper-triangle Hessian/Fisher]."""
     rois = np.ascontiguousarray(rois, dtype=np.float64)
@@ -123,8 +123,12 @@ def _eval_entry(self, rois, fittype, coeff, theta, fisher=False):
     th = np.ascontiguousarray(np.asarray(theta, np.float64)[:, :nv].T)
     out = np.zeros((n, 1 + nv + nv * (nv + 1) // 2), np.float64)
     fn = getattr(self._lib, f"oracle_eval{fittype}_f64")
-    fn(_ptr(rois, np.float64), _ptr(coeff, np.float64), *[_i(d) for d in dims], _i(s), _i(n),
-       _ptr(th, np.float64), _i(int(fisher)), _ptr(out, np.float64))
+    args = [_ptr(rois, np.float64), _ptr(coeff, np.float64)]
+    if fittype == 8:
+        c3 = np.ascontiguousarray(coeff3, dtype=np.float64)
+        args.append(_ptr(c3, np.float64))
+    fn(*args, *[_i(d) for d in dims], _i(s), _i(n), _ptr(th, np.float64), _i(int(fisher)),
+       _ptr(out, np.float64))
     return out
 
 

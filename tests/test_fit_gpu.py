@@ -82,7 +82,7 @@ def degenerate_rois(oracle, d):
     return out
 
 
-@pytest.mark.parametrize("case", [c for c in golden_cases() if not c.startswith("m8")])
+@pytest.mark.parametrize("case", golden_cases())
 def test_golden_fixture(bsfit_mod, oracle, case):
     d = np.load(os.path.join(GOLDEN, case + ".npz"))
     ft = int(d["fittype"])
@@ -108,7 +108,7 @@ def test_golden_fixture(bsfit_mod, oracle, case):
     # for these small cases (one in 4 for fit type 7, whose "let it go" switch
     # and 1e-5 initial w clamp make its trajectory far more rounding-sensitive:
     # the reference's own FP32 and FP64 builds agree on only a third of 4D ROIs).
-    slack = max(1, keep.sum() // (4 if ft == 7 else 8))
+    slack = max(1, keep.sum() // (4 if ft in (7, 8) else 8))
     assert ok[keep].sum() >= ok32[keep].sum() - slack, (
         case, ok[keep].mean(), ok32[keep].mean(), np.where(keep & ~ok)[0])
     # Iteration counts are integers in the last column.
@@ -124,21 +124,24 @@ def test_special_rois_no_crash(bsfit_mod):
     assert np.array_equal(np.isnan(P[:, :5]), np.isnan(R[:, :5]))
 
 
-@pytest.mark.parametrize("fittype,n,min_frac", [(6, 20000, 0.955), (7, 3000, 0.33)])
+@pytest.mark.parametrize("fittype,n,min_frac", [(6, 20000, 0.955), (7, 3000, 0.33), (8, 320, 0.0)])
 def test_parity_at_scale(bsfit_mod, oracle, fittype, n, min_frac):
     from bsfit import workloads as W
     if fittype == 6:
         wl = W.workload_3d(n, s=13, stream=501)
-    else:
+    elif fittype == 7:
         wl = W.workload_4d(n, sizes=(13,), stream=502)[0]
-    nv = {6: 5, 7: 6}[fittype]
+    else:
+        wl = W.workload_5d(n, stream=503)
+    nv = {6: 5, 7: 6, 8: 8}[fittype]
     kw = {"initP": wl.init_p} if wl.init_p is not None else {}
+    if wl.coeff3 is not None:
+        kw["coeff3"] = wl.coeff3
     P, C, L = bsfit_mod.GPUmleFit_LM_multiD(wl.rois, fittype, wl.iterations, wl.coeff, **kw)
     threads = os.cpu_count() or 1
-    R, RC, RL = oracle.fit(wl.rois, fittype, wl.iterations, wl.coeff, init_p=wl.init_p,
-                           precision="f64", threads=threads)
-    S, SC, SL = oracle.fit(wl.rois, fittype, wl.iterations, wl.coeff, init_p=wl.init_p,
-                           precision="f32", threads=threads)
+    okw = dict(init_p=wl.init_p, coeff3=wl.coeff3, threads=threads)
+    R, RC, RL = oracle.fit(wl.rois, fittype, wl.iterations, wl.coeff, precision="f64", **okw)
+    S, SC, SL = oracle.fit(wl.rois, fittype, wl.iterations, wl.coeff, precision="f32", **okw)
     ok = tol_pass(P, C, R, RC, nv)
     ok32 = tol_pass(S, SC, R, RC, nv)
     assert ok.mean() >= min_frac, ok.mean()
@@ -176,22 +179,29 @@ def test_eval_matches_oracle_at_fixed_parameters(bsfit_mod, oracle):
     sqrt(H_kk H_ll) (with a floor of 1e-6 of the column median, so an
     identically zero curvature on a boundary knot does not divide by zero)."""
     import torch
-    for case in ("m6_basic", "m7_basic"):
+    for case in ("m6_basic", "m7_basic", "m8_basic"):
         d = np.load(os.path.join(GOLDEN, case + ".npz"))
         ft = int(d["fittype"])
-        nv = {6: 5, 7: 6}[ft]
+        nv = {6: 5, 7: 6, 8: 8}[ft]
         theta = d["f64_P"][:, :nv].astype(np.float32)
-        m = bsfit_mod.Model(ft, d["coeff"], init_p=d["init_p"] if "init_p" in d else None)
+        c3 = d["coeff3"] if "coeff3" in d else None
+        m = bsfit_mod.Model(ft, d["coeff"], coeff3=c3, init_p=d["init_p"] if "init_p" in d else None)
         r = torch.from_numpy(d["rois"]).cuda()
         th = torch.from_numpy(np.ascontiguousarray(theta.T)).cuda()
         idx = [(l, k) for l in range(nv) for k in range(l, nv)]
         for fisher in (False, True):
             g = m.eval_torch(r, th, fisher=fisher).cpu().numpy().astype(np.float64)
-            ref = oracle.eval(d["rois"], ft, d["coeff"], theta.astype(np.float64), fisher=fisher)
+            ref = oracle.eval(d["rois"], ft, d["coeff"], theta.astype(np.float64), fisher=fisher,
+                              coeff3=c3)
             diag = np.stack([ref[:, 1 + nv + idx.index((k, k))] for k in range(nv)], 1)
             diag = np.maximum(diag, 1e-6 * np.median(diag, 0))
             e0 = np.abs(g[:, 0] - ref[:, 0]).max() / np.abs(ref[:, 0]).max()
-            eJ = (np.abs(g[:, 1:1 + nv] - ref[:, 1:1 + nv]) / np.sqrt(diag)).max()
-            eH = max((np.abs(g[:, 1 + nv + i] - ref[:, 1 + nv + i]) /
-                      np.sqrt(diag[:, l] * diag[:, k])).max() for i, (l, k) in enumerate(idx))
-            assert e0 < 1e-5 and eJ < 1e-3 and eH < 1e-3, (case, fisher, e0, eJ, eH)
+            eJc = (np.abs(g[:, 1:1 + nv] - ref[:, 1:1 + nv]) / np.sqrt(diag)).max(0)
+            eHc = [(np.abs(g[:, 1 + nv + i] - ref[:, 1 + nv + i]) /
+                    np.sqrt(diag[:, l] * diag[:, k])).max() for i, (l, k) in enumerate(idx)]
+            # The 5D mixture sums 64 coefficients per node and two correction
+            # maps; its FP32 derivative error is a few 1e-3 of the curvature
+            # scale where a curvature is small.
+            tol = 1e-3 if ft != 8 else 1e-2
+            assert e0 < 1e-5 and eJc.max() < tol and max(eHc) < tol, (
+                case, fisher, e0, eJc.round(5).tolist(), np.round(eHc, 5).tolist())

@@ -144,6 +144,51 @@ class Model:
             pass
 
 
+class Batch:
+    """Batched fit of ROI segments (mixed ROI sizes and models) with one
+    persistent launch per fit type. Each entry: (model, rois_cuda_tensor,
+    iterations). Outputs are allocated once and reused across calls; the work
+    queue lives in a small device scratch buffer owned by the batch."""
+
+    def __init__(self, entries, device=None):
+        import torch
+        if not 0 < len(entries) <= 48:
+            raise ValueError("a batch holds 1 to 48 segments")
+        self.entries = list(entries)
+        dev = device or self.entries[0][1].device
+        self.outputs = []
+        segs = (_native.Segment * len(self.entries))()
+        for k, (m, r, it) in enumerate(self.entries):
+            n, s = r.shape[0], r.shape[-1]
+            P = torch.empty((m.nv + 1, n), device=dev)
+            C = torch.empty((m.nv, n), device=dev)
+            L = torch.empty((n,), device=dev)
+            self.outputs.append((P, C, L))
+            segs[k].model = m._h.value
+            segs[k].d_rois = r.data_ptr()
+            segs[k].roi_size = s
+            segs[k].nfits = n
+            segs[k].iterations = int(it)
+            segs[k].d_P, segs[k].d_CRLB, segs[k].d_LL = P.data_ptr(), C.data_ptr(), L.data_ptr()
+        self._segs = segs
+        nb = _native.lib().bsfit_batch_scratch_bytes(len(self.entries))
+        self.scratch = torch.zeros((max(nb, 256) // 8,), dtype=torch.int64, device=dev)
+
+    def run(self, stream=None):
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream(self.scratch.device)
+        check(_native.lib().bsfit_batch_fit_device(
+            np.ctypeslib.ctypes.cast(self._segs, np.ctypeslib.ctypes.c_void_p), len(self.entries),
+            self.scratch.data_ptr(), self.scratch.numel() * 8, st.cuda_stream), "bsfit_batch_fit_device")
+        return self.outputs
+
+    def counters(self):
+        """(claimed, finished) ROI counts per segment after completion."""
+        c = self.scratch.cpu().numpy()
+        k = len(self.entries)
+        return c[:k].copy(), c[k:2 * k].copy()
+
+
 def measure_fp32_peak():
     """Measured FP32 FMA throughput of the current device, TFLOP/s."""
     v = np.ctypeslib.ctypes.c_double()

@@ -33,6 +33,9 @@ SIGNATURES = {
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
         ctypes.c_int32, ctypes.c_void_p]),
+    "bsfit_batch_scratch_bytes": (ctypes.c_int64, [ctypes.c_int32]),
+    "bsfit_batch_fit_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "bsfit_fit_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -42,9 +45,10 @@ SIGNATURES = {
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
-            raise ImportError(f"{LIB} is not built: run __graft_entry__.build() first")
-        handle = ctypes.CDLL(LIB)
+        path = os.environ.get("BSFIT_LIB", LIB)  # an alternative build of the same library
+        if not os.path.exists(path):
+            raise ImportError(f"{path} is not built: run __graft_entry__.build() first")
+        handle = ctypes.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(handle, name)
             fn.restype = res
@@ -63,3 +67,11 @@ class BsfitError(RuntimeError):
 def check(status, where=""):
     if status != 0:
         raise BsfitError(status, where)
+
+
+class Segment(ctypes.Structure):
+    """bsfit_segment (include/bsfit.h)."""
+    _fields_ = [("model", ctypes.c_void_p), ("d_rois", ctypes.c_void_p),
+                ("roi_size", ctypes.c_int64), ("nfits", ctypes.c_int64),
+                ("iterations", ctypes.c_int32), ("d_P", ctypes.c_void_p),
+                ("d_CRLB", ctypes.c_void_p), ("d_LL", ctypes.c_void_p)]

@@ -232,6 +232,73 @@ int bsfit_eval_device(bsfit_model model, const float* d_rois, int64_t roi_size, 
   return cuda_status(bsfit::launch_eval(a, d_theta, d_out, fisher, (cudaStream_t)stream));
 }
 
+int64_t bsfit_batch_scratch_bytes(int32_t nseg) {
+  if (nseg < 0) return 0;
+  return (((int64_t)nseg * 2 * 8) + 255) / 256 * 256;
+}
+
+int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scratch,
+                           int64_t scratch_bytes, void* stream) {
+  if (nseg < 0 || nseg > BSFIT_MAX_SEGMENTS) return BSFIT_E_INVALID;
+  if (nseg == 0) return BSFIT_OK;
+  if (!segs || !d_scratch || scratch_bytes < bsfit_batch_scratch_bytes(nseg)) return BSFIT_E_INVALID;
+  for (int i = 0; i < nseg; ++i) {
+    const bsfit_segment& g = segs[i];
+    if (!g.model) return BSFIT_E_INVALID;
+    if (g.roi_size < 1 || g.roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+    if (g.nfits < 0) return BSFIT_E_INVALID;
+    if (g.nfits > 0 && (!g.d_rois || !g.d_P || !g.d_CRLB || !g.d_LL)) return BSFIT_E_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long* next = (unsigned long long*)d_scratch;
+  unsigned long long* done = next + nseg;
+  cudaError_t e = cudaMemsetAsync(d_scratch, 0, (size_t)nseg * 2 * 8, st);
+  if (e != cudaSuccess) return cuda_status(e);
+  // One persistent launch per fit type; within it, segments by decreasing
+  // cost (pixels x iteration cap) so the longest fits start first.
+  for (int mode = 6; mode <= 8; ++mode) {
+    bsfit::BatchArgs a;
+    std::memset(&a, 0, sizeof(a));
+    int order[BSFIT_MAX_SEGMENTS];
+    int k = 0;
+    for (int i = 0; i < nseg; ++i)
+      if (segs[i].model->dev.fittype == mode && segs[i].nfits > 0) order[k++] = i;
+    if (k == 0) continue;
+    for (int x = 1; x < k; ++x)
+      for (int y = x; y > 0; --y) {
+        const bsfit_segment& p0 = segs[order[y - 1]];
+        const bsfit_segment& p1 = segs[order[y]];
+        if (p0.roi_size * p0.roi_size * (int64_t)p0.iterations <
+            p1.roi_size * p1.roi_size * (int64_t)p1.iterations) {
+          int t = order[y - 1];
+          order[y - 1] = order[y];
+          order[y] = t;
+        }
+      }
+    a.nseg = k;
+    a.next = next;
+    a.done = done;
+    a.flags = 0;
+    for (int j = 0; j < k; ++j) {
+      const bsfit_segment& g = segs[order[j]];
+      bsfit::BatchSeg& b = a.seg[j];
+      b.m = g.model->dev;
+      b.rois = g.d_rois;
+      b.P = g.d_P;
+      b.CRLB = g.d_CRLB;
+      b.LL = g.d_LL;
+      b.n = g.nfits;
+      b.s = (int)g.roi_size;
+      b.iterations = g.iterations;
+      b.slot = order[j];  // counters stay in the caller's segment order
+      if (b.s > a.s_max) a.s_max = b.s;
+    }
+    e = bsfit::launch_batch(a, mode, st);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  return BSFIT_OK;
+}
+
 int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t roi_size2,
                               int64_t nfits, int32_t fittype, int32_t iterations,
                               const float* coeff, int32_t coeff_ndim, const int64_t* coeff_dims,

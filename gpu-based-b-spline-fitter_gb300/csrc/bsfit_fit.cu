@@ -36,7 +36,34 @@
 #include "bsfit_device.cuh"
 #include "bsfit_internal.h"
 
+// Minimum resident blocks per SM requested for the 3D kernels (4 warps each):
+// trades registers for occupancy.
+#ifndef BSFIT_MINBLOCKS6
+#define BSFIT_MINBLOCKS6 4
+#endif
+
 namespace bsfit {
+
+// Optional phase timing (diagnostic builds with -DBSFIT_PHASE_TIMING): lane 0
+// of every warp adds the clock64() cycles spent in each phase of the fit.
+#ifdef BSFIT_PHASE_TIMING
+__device__ unsigned long long g_phase_cycles[16];
+#define PHASE_BEGIN() long long _ph_t0 = clock64()
+#define PHASE_MARK(k)                                                     \
+  do {                                                                    \
+    long long _ph_t1 = clock64();                                         \
+    if ((threadIdx.x & 31) == 0)                                          \
+      atomicAdd(&g_phase_cycles[k], (unsigned long long)(_ph_t1 - _ph_t0)); \
+    _ph_t0 = _ph_t1;                                                      \
+  } while (0)
+#else
+#define PHASE_BEGIN() \
+  do {                \
+  } while (0)
+#define PHASE_MARK(k) \
+  do {                \
+  } while (0)
+#endif
 
 template <int MODE>
 struct ModeTraits;
@@ -144,6 +171,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
   float* G = ws + L.off_g();
   const int wp = L.wp;
   __syncwarp();  // the previous evaluation's readers of kxs / w / G are done
+  PHASE_BEGIN();
 
   // Positions (CPUmleFit_LM.cpp:2512-2523): pixel jj sits at
   // (xc + jj) + off along X, pixel ii at (yc + ii) + off along Y.
@@ -195,6 +223,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
   const int kz = knot_index(zc, m.n[2]);
   const int kw = (D >= 4) ? knot_index(wc, m.n[3]) : 0;
   const int ku = (D >= 5) ? knot_index(uc, m.n[4]) : 0;
+  PHASE_MARK(0);
 
   // (A) Non-lateral contraction at every lateral node of the window.
   {
@@ -341,6 +370,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
     }
   }
   __syncwarp();
+  PHASE_MARK(1);
 
   // (B) Y contraction for every (X node, pixel row ii).
   {
@@ -384,6 +414,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
     }
   }
   __syncwarp();
+  PHASE_MARK(2);
 
   // (C) X contraction per pixel, fused with the likelihood sums.
   FPair err{0.0f, 0.0f};
@@ -499,9 +530,11 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
       }
     }
   }
+  PHASE_MARK(3);
   warp_sum_array<NV>(jac);
   warp_sum_array<NH>(hes);
   err_out = warp_sum_pair(err);
+  PHASE_MARK(4);
 }
 
 // ---------------------------------------------------------------------------
@@ -614,6 +647,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   for (int p = lane; p < s2; p += 32) data[p] = __ldg(src + p);
   __syncwarp();
 
+  PHASE_BEGIN();
   // Initial guesses (CPUgaussLib.cpp:172-225, CPUmleFit_LM.cpp:2477-2482).
   float th[NV];
   {
@@ -714,6 +748,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   int kk = 0;
   bool need_eval = true, first = true, fisher = false;
   FPair ll{0.0f, 0.0f};
+  PHASE_MARK(5);
   for (;;) {
     if (need_eval) {
       FPair e;
@@ -731,6 +766,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
         break;
       }
       err = e;
+      PHASE_BEGIN();
     }
     if (kk >= a.iterations) {
       fisher = true;
@@ -926,6 +962,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
       rec[22] = e_n;
     }
     ++kk;
+    PHASE_MARK(6);
   }
 
   // CRLB and log-likelihood at the final theta (the Fisher pass above).
@@ -935,7 +972,11 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   for (int l = 0; l < NV; ++l)
 #pragma unroll
     for (int mm = l; mm < NV; ++mm) M[l * NV + mm] = M[mm * NV + l] = (double)fm[hidx<NV>(l, mm)];
-  mat_inv_diag<NV>(M, diag);
+  {
+    PHASE_BEGIN();
+    mat_inv_diag<NV>(M, diag);
+    PHASE_MARK(7);
+  }
   if (lane == 0) {
     const int64_t n = a.out_n;
     const int64_t o = a.out_offset + roi;
@@ -950,7 +991,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(128) fit_kernel(FitArgs a) {
+__global__ void __launch_bounds__(128, (MODE == 6 ? BSFIT_MINBLOCKS6 : 1)) fit_kernel(FitArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
   const WarpLayout L = make_layout(MODE, a.s);
@@ -961,6 +1002,86 @@ __global__ void __launch_bounds__(128) fit_kernel(FitArgs a) {
   const int64_t total_warps = (int64_t)gridDim.x * wpb;
   for (int64_t roi = (int64_t)blockIdx.x * wpb + wib; roi < a.nfits; roi += total_warps)
     fit_roi<MODE>(a, L, ws, lane, roi);
+}
+
+// Persistent batched fit: every warp claims ROIs one at a time from the
+// segments' work counters (in segment order: the host sorts segments by
+// decreasing cost, so the largest ROIs start first and the tail is short),
+// fits them, and counts them done. The warp's shared memory is laid out for
+// the largest ROI of the batch.
+template <int MODE>
+__global__ void __launch_bounds__(128, (MODE == 6 ? BSFIT_MINBLOCKS6 : 1)) batch_kernel(const __grid_constant__ BatchArgs a) {
+  extern __shared__ float4 smem4[];
+  float* smem = reinterpret_cast<float*>(smem4);
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  float* ws = smem + wib * make_layout(MODE, a.s_max).total();
+  int seg = 0;
+  while (seg < a.nseg) {
+    const BatchSeg& g = a.seg[seg];
+    unsigned long long i = 0;
+    if (lane == 0) i = atomicAdd(&a.next[g.slot], 1ull);
+    i = __shfl_sync(kFull, i, 0);
+    if ((int64_t)i >= g.n) {
+      ++seg;
+      continue;
+    }
+    FitArgs fa;
+    fa.m = g.m;
+    fa.rois = g.rois;
+    fa.s = g.s;
+    fa.nfits = g.n;
+    fa.iterations = g.iterations;
+    fa.P = g.P;
+    fa.CRLB = g.CRLB;
+    fa.LL = g.LL;
+    fa.out_n = g.n;
+    fa.out_offset = 0;
+    fa.trace = nullptr;
+    fa.trace_max = 0;
+    fa.flags = a.flags;
+    fit_roi<MODE>(fa, make_layout(MODE, g.s), ws, lane, (int64_t)i);
+    if (lane == 0) atomicAdd(&a.done[g.slot], 1ull);
+  }
+}
+
+cudaError_t launch_batch(const BatchArgs& a, int mode, cudaStream_t stream) {
+  if (a.nseg <= 0) return cudaSuccess;
+  const int per_warp = warp_smem_floats(mode, a.s_max) * 4;
+  void (*kern)(const BatchArgs) = nullptr;
+  if (mode == 6) kern = batch_kernel<6>;
+  else if (mode == 7) kern = batch_kernel<7>;
+  else if (mode == 8) kern = batch_kernel<8>;
+  else return cudaErrorInvalidValue;
+  int wpb = 4, blocks_per_sm = 0, best = -1;
+  for (int cand = 4; cand >= 1; cand >>= 1) {
+    const int sm = per_warp * cand;
+    if (sm > 220 * 1024) continue;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
+      continue;
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * cand, sm) != cudaSuccess) continue;
+    if (b * cand > best) {
+      best = b * cand;
+      wpb = cand;
+      blocks_per_sm = b;
+    }
+  }
+  if (best <= 0) return cudaErrorInvalidConfiguration;
+  const int smem = per_warp * wpb;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t total = 0;
+  for (int i = 0; i < a.nseg; ++i) total += a.seg[i].n;
+  int64_t grid = (int64_t)sms * blocks_per_sm;
+  const int64_t need = (total + wpb - 1) / wpb;
+  if (need < grid) grid = need;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(a);
+  return cudaGetLastError();
 }
 
 // One evaluation per ROI at caller-given parameters: writes, per ROI, the
@@ -1111,3 +1232,14 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
 }
 
 }  // namespace bsfit
+
+#ifdef BSFIT_PHASE_TIMING
+extern "C" int bsfit_debug_phase_cycles(unsigned long long* out, int reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, bsfit::g_phase_cycles, sizeof(unsigned long long) * 16);
+  if (reset) {
+    unsigned long long z[16] = {0};
+    cudaMemcpyToSymbol(bsfit::g_phase_cycles, z, sizeof(z));
+  }
+  return (int)e;
+}
+#endif

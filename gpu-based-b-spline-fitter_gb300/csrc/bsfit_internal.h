@@ -41,7 +41,34 @@ struct FitArgs {
 constexpr int TRACE_REC = 32;
 constexpr int FLAG_NO_REFINE = 1;  // skip the refinement step of the LM solve
 
+// Batched form: ROI segments of one fit type fitted by one persistent launch.
+constexpr int kMaxBatchSegs = 48;
+
+struct BatchSeg {
+  ModelDev m;
+  const float* rois;
+  float* P;
+  float* CRLB;
+  float* LL;
+  int64_t n;
+  int s;
+  int iterations;
+  int slot;  // index of this segment's counters in next[] / done[]
+};
+
+struct BatchArgs {
+  int nseg;
+  int s_max;
+  int flags;
+  // Work queue in caller-provided device scratch: next[i] is the next
+  // unclaimed ROI of segment i, done[i] counts its finished ROIs.
+  unsigned long long* next;
+  unsigned long long* done;
+  BatchSeg seg[kMaxBatchSegs];
+};
+
 int warp_smem_floats(int mode, int s);
+cudaError_t launch_batch(const BatchArgs& a, int mode, cudaStream_t stream);
 cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream);
 cudaError_t measure_fp32_peak(double* tflops);
 cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fisher,

@@ -148,6 +148,39 @@ int bsfit_trace_device(bsfit_model model, const float* d_rois, int64_t roi_size,
                        int32_t iterations, int32_t flags, float* d_P, float* d_CRLB, float* d_LL,
                        float* d_trace, int32_t trace_max, void* stream);
 
+/*
+ * Batched form (no counterpart in the reference, whose callers loop over blocks
+ * of 20,000 / 5,000 ROIs and call the mex once per block and start,
+ * MultiD_fitter/simplefitter_cspline.m:309-313,463-524): segments of ROIs,
+ * each with its own model, ROI size, iteration cap and output buffers, fitted
+ * by one persistent launch per fit type with a device work queue. Segments may
+ * mix ROI sizes and models; fit types are launched one after the other on the
+ * stream. At most BSFIT_MAX_SEGMENTS segments per call.
+ */
+#define BSFIT_MAX_SEGMENTS 48
+
+typedef struct bsfit_segment {
+  bsfit_model model;
+  const float* d_rois;   /* device, nfits * roi_size^2 floats */
+  int64_t roi_size;
+  int64_t nfits;
+  int32_t iterations;
+  float* d_P;            /* device outputs, column-major, leading dimension nfits */
+  float* d_CRLB;
+  float* d_LL;
+} bsfit_segment;
+
+/* Bytes of device scratch bsfit_batch_fit_device needs for nseg segments
+ * (two 64-bit counters per segment, 256-byte aligned). */
+int64_t bsfit_batch_scratch_bytes(int32_t nseg);
+
+/* Asynchronous batched fit on a stream. d_scratch: caller-provided device
+ * memory of at least bsfit_batch_scratch_bytes(nseg) bytes, zeroed by the
+ * call itself (stream-ordered); after completion it holds, per segment, the
+ * number of claimed and of finished ROIs. Allocates nothing. */
+int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scratch,
+                           int64_t scratch_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

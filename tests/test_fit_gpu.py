@@ -205,3 +205,39 @@ def test_eval_matches_oracle_at_fixed_parameters(bsfit_mod, oracle):
             tol = 1e-3 if ft != 8 else 1e-2
             assert e0 < 1e-5 and eJc.max() < tol and max(eHc) < tol, (
                 case, fisher, e0, eJc.round(5).tolist(), np.round(eHc, 5).tolist())
+
+
+def test_batch_matches_plain(bsfit_mod):
+    """Segments of mixed ROI sizes and fit types in one batched call give the
+    same results as one plain call per segment, and every ROI is claimed and
+    finished exactly once."""
+    import torch
+    from bsfit import workloads as W
+    g3 = W.workload_3d_mixed(3000, sizes=(11, 13, 17), ratio=(1, 2, 1), stream=601)
+    g4 = W.workload_4d(400, sizes=(13,), stream=602)[0]
+    g5 = W.workload_5d(40, stream=603)
+    m3 = bsfit_mod.Model(6, g3[0].coeff)
+    m4 = bsfit_mod.Model(7, g4.coeff, init_p=g4.init_p)
+    m5 = bsfit_mod.Model(8, g5.coeff, coeff3=g5.coeff3, init_p=g5.init_p)
+    entries = [(m3, torch.from_numpy(g.rois).cuda(), g.iterations) for g in g3]
+    entries.append((m4, torch.from_numpy(g4.rois).cuda(), g4.iterations))
+    entries.append((m5, torch.from_numpy(g5.rois).cuda(), g5.iterations))
+    b = bsfit_mod.Batch(entries)
+    outs = b.run()
+    torch.cuda.synchronize()
+    claimed, finished = b.counters()
+    n = np.array([e[1].shape[0] for e in entries])
+    assert np.all(finished == n) and np.all(claimed >= n)
+    for (m, r, it), (P, C, L) in zip(entries, outs):
+        Pp, Cp, Lp = m.fit_torch(r, it)
+        torch.cuda.synchronize()
+        assert np.array_equal(P.cpu().numpy(), Pp.cpu().numpy(), equal_nan=True)
+        assert np.array_equal(C.cpu().numpy(), Cp.cpu().numpy(), equal_nan=True)
+        assert np.array_equal(L.cpu().numpy(), Lp.cpu().numpy(), equal_nan=True)
+
+
+def test_batch_rejects_bad_arguments(bsfit_mod):
+    from bsfit import _native
+    lib = _native.lib()
+    assert lib.bsfit_batch_fit_device(None, 49, None, 0, None) == 11
+    assert lib.bsfit_batch_scratch_bytes(3) == 256

@@ -36,6 +36,7 @@ SIGNATURES = {
     "bsfit_batch_scratch_bytes": (ctypes.c_int64, [ctypes.c_int32]),
     "bsfit_batch_fit_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    "bsfit_batch_fit_device_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
     "bsfit_fit_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),

@@ -104,6 +104,8 @@ const char* bsfit_status_str(int status) {
     case BSFIT_E_INIT_P: return "initP missing or too short for this fit type";
     case BSFIT_E_INVALID: return "invalid argument";
     case BSFIT_E_TIMEOUT: return "bounded device wait timed out";
+    case BSFIT_E_STATIC_LIMIT:
+      return "too many segments for the allocation-free entry point (its fixed scratch holds 48)";
     default: return "unknown status";
   }
 }

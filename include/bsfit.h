@@ -55,7 +55,9 @@ typedef enum bsfit_status {
   /* invalid handle or argument of the device-level API */
   BSFIT_E_INVALID = 11,
   /* a bounded device-side wait ran out (batched / serving forms) */
-  BSFIT_E_TIMEOUT = 12
+  BSFIT_E_TIMEOUT = 12,
+  /* more segments than the allocation-free entry point's fixed scratch holds */
+  BSFIT_E_STATIC_LIMIT = 13
 } bsfit_status;
 
 /* Human-readable text of a status code (replaces mexErrMsgIdAndTxt texts). */
@@ -180,6 +182,22 @@ int64_t bsfit_batch_scratch_bytes(int32_t nseg);
  * number of claimed and of finished ROIs. Allocates nothing. */
 int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scratch,
                            int64_t scratch_bytes, void* stream);
+
+/*
+ * Allocation-free batched fit (no counterpart in the reference). For callers
+ * that cannot allocate device memory when they fit - a fixed-rate acquisition
+ * loop, where cudaMalloc may synchronise the device, or an application that
+ * reserved the GPU's memory for its own pool - this variant of
+ * bsfit_batch_fit_device keeps the work-queue counters in a fixed device array
+ * inside the library instead of caller scratch, and allocates nothing.
+ * Limit: BSFIT_STATIC_MAX_SEGMENTS segments per call (BSFIT_E_STATIC_LIMIT
+ * beyond). The array is shared by all calls on a device: each call zeroes the
+ * counters it uses before its launch, and calls that overlap on the GPU race
+ * on them, so serialise such calls. The first call on each device looks the
+ * array's address up (cudaGetSymbolAddress); make it before any stream capture.
+ */
+#define BSFIT_STATIC_MAX_SEGMENTS 48
+int bsfit_batch_fit_device_static(const bsfit_segment* segs, int32_t nseg, void* stream);
 
 #ifdef __cplusplus
 }

@@ -36,7 +36,7 @@ def test_binding_matches_header():
 
 
 def test_status_strings(lib):
-    for st in range(0, 13):
+    for st in range(0, 14):
         assert lib.bsfit_status_str(st)
     assert b"square" in lib.bsfit_status_str(4)
 

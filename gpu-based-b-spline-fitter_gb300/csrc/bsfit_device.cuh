@@ -31,46 +31,42 @@ __device__ __forceinline__ int knot_index(float pos, int n) {
   return c;
 }
 
-// Centred cubic B-spline with the reference's half-open intervals
-// (CPUsplineLib.cpp:1311-1324).
-__device__ __forceinline__ float bspline3(float x) {
-  float x2 = x * x;
-  float x3 = x2 * x;
-  if (x >= 1.0f && x < 2.0f) return 4.0f / 3.0f - 2.0f * x + x2 - 1.0f / 6.0f * x3;
-  if (x >= 0.0f && x < 1.0f) return 2.0f / 3.0f - x2 + 0.5f * x3;
-  if (x >= -1.0f && x < 0.0f) return 2.0f / 3.0f - x2 - 0.5f * x3;
-  if (x >= -2.0f && x < -1.0f) return 4.0f / 3.0f + 2.0f * x + x2 + 1.0f / 6.0f * x3;
-  return 0.0f;
+// Branch-free forms of the two bases. With a = |x| the reference's half-open
+// pieces are B3 = 2/3 - a^2 + a^3/2 (a < 1), (2 - a)^3 / 6 (1 <= a < 2), 0, and
+// B2 = 3/4 - a^2 (a < 1/2), (3/2 - a)^2 / 2 (1/2 <= a < 3/2), 0; they agree
+// with the reference's intervals at every boundary (both sides give the same
+// value there).
+__device__ __forceinline__ float bspline3_sym(float x) {
+  const float a = fabsf(x);
+  const float a2 = a * a;
+  const float inner = fmaf(0.5f * a, a2, 2.0f / 3.0f - a2);
+  const float b = 2.0f - a;
+  const float outer = b * b * b * (1.0f / 6.0f);
+  return (a < 1.0f) ? inner : ((a < 2.0f) ? outer : 0.0f);
 }
 
-// Centred quadratic B-spline, the derivative basis (CPUsplineLib.cpp:1296-1309).
-__device__ __forceinline__ float bspline2(float x) {
-  float x2 = x * x;
-  if (x >= 0.5f && x < 1.5f) return 1.125f - 1.5f * x + 0.5f * x2;
-  if (x >= -0.5f && x < 0.5f) return 0.75f - x2;
-  if (x >= -1.5f && x < -0.5f) return 1.125f + 1.5f * x + 0.5f * x2;
-  return 0.0f;
+__device__ __forceinline__ float bspline2_sym(float x) {
+  const float a = fabsf(x);
+  const float inner = 0.75f - a * a;
+  const float b = 1.5f - a;
+  const float outer = 0.5f * b * b;
+  return (a < 0.5f) ? inner : ((a < 1.5f) ? outer : 0.0f);
 }
 
-// One of the seven 1-D weights of an axis, indexed j = 0..6:
-//   j = 0..3: value weight of the node at offset j - 1 from the floor knot,
-//   j = 4..6: derivative weight of the node difference C[o + 1] - C[o] at
-//             offset o = j - 5.
-// The argument expressions follow the reference's loop form
-// (CPUsplineLib.cpp:1138-1158): side 1 uses B3(t + v - 1), B2(t - 1 + v - 1/2)
-// for the nodes at offsets 1 - v; side 2 uses B3(t - v), B2(t - 1 - v + 1/2)
-// for offsets v. The derivative weight of offset +2 is identically zero.
+// One of the seven 1-D weights of an axis at fractional position t, indexed
+// j = 0..6:
+//   j = 0..3: value weight B3(t - o) of the node at offset o = j - 1 from the
+//             floor knot,
+//   j = 4..6: derivative weight B2(t - o - 1/2) of the node difference
+//             C[o + 1] - C[o] at offset o = j - 5.
+// These are the reference's loop forms (CPUsplineLib.cpp:1138-1158: side 1
+// B3(t + v - 1), B2(t - 1 + v - 1/2) at offsets 1 - v; side 2 B3(t - v),
+// B2(t - 1 - v + 1/2) at offsets v) with the argument formed in one rounding.
+// The derivative weight of offset +2 is identically zero.
 __device__ __forceinline__ float axis_weight(float t, int j) {
-  float dt = t - 1.0f;
-  switch (j) {
-    case 0: return bspline3((t + 2.0f) - 1.0f);         // offset -1 (side 1, v = 2)
-    case 1: return bspline3((t + 1.0f) - 1.0f);         // offset  0 (side 1, v = 1)
-    case 2: return bspline3(t - 1.0f);                  // offset +1 (side 2, v = 1)
-    case 3: return bspline3(t - 2.0f);                  // offset +2 (side 2, v = 2)
-    case 4: return bspline2((dt + 2.0f) - 0.5f);        // offset -1
-    case 5: return bspline2((dt + 1.0f) - 0.5f);        // offset  0
-    default: return bspline2((dt - 1.0f) + 0.5f);       // offset +1
-  }
+  const float off = (j < 4) ? (float)(j - 1) : (float)(j - 5) + 0.5f;
+  const float x = t - off;
+  return (j < 4) ? bspline3_sym(x) : bspline2_sym(x);
 }
 
 // ---------------------------------------------------------------------------
@@ -82,17 +78,9 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-__device__ __forceinline__ int warp_min(int v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(kFull, v, o));
-  return v;
-}
+__device__ __forceinline__ int warp_min(int v) { return __reduce_min_sync(kFull, v); }
 
-__device__ __forceinline__ int warp_max(int v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
-  return v;
-}
+__device__ __forceinline__ int warp_max(int v) { return __reduce_max_sync(kFull, v); }
 
 template <int K>
 __device__ __forceinline__ void warp_sum_array(float (&v)[K]) {

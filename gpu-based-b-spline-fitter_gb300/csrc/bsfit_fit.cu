@@ -48,16 +48,20 @@ namespace bsfit {
 // of every warp adds the clock64() cycles spent in each phase of the fit.
 #ifdef BSFIT_PHASE_TIMING
 __device__ unsigned long long g_phase_cycles[16];
-#define PHASE_BEGIN() long long _ph_t0 = clock64()
-#define PHASE_MARK(k)                                                     \
-  do {                                                                    \
-    long long _ph_t1 = clock64();                                         \
-    if ((threadIdx.x & 31) == 0)                                          \
+#define PHASE_DECL() long long _ph_t0 = clock64()
+#define PHASE_RESET() _ph_t0 = clock64()
+#define PHASE_MARK(k)                                                       \
+  do {                                                                      \
+    long long _ph_t1 = clock64();                                           \
+    if ((threadIdx.x & 31) == 0)                                            \
       atomicAdd(&g_phase_cycles[k], (unsigned long long)(_ph_t1 - _ph_t0)); \
-    _ph_t0 = _ph_t1;                                                      \
+    _ph_t0 = _ph_t1;                                                        \
   } while (0)
 #else
-#define PHASE_BEGIN() \
+#define PHASE_DECL() \
+  do {               \
+  } while (0)
+#define PHASE_RESET() \
   do {                \
   } while (0)
 #define PHASE_MARK(k) \
@@ -171,7 +175,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
   float* G = ws + L.off_g();
   const int wp = L.wp;
   __syncwarp();  // the previous evaluation's readers of kxs / w / G are done
-  PHASE_BEGIN();
+  PHASE_DECL();
 
   // Positions (CPUmleFit_LM.cpp:2512-2523): pixel jj sits at
   // (xc + jj) + off along X, pixel ii at (yc + ii) + off along Y.
@@ -590,50 +594,53 @@ __device__ __forceinline__ void chol_solve(const float (&u)[NV * NV], const floa
   }
 }
 
-// Unpivoted LU inverse diagonal in FP64 (VC/CPUmleFit_LM/MatInvLib.h:17-77).
-// A parameter whose model derivative is exactly zero at every pixel (z on the
-// mirror-padded boundary knot, for instance) has an exactly zero Fisher row and
-// column. The reference's FP64 arithmetic turns that into a huge finite
-// variance from rounding noise; here the row is decoupled explicitly: its
-// diagonal is set to the smallest positive double, so its variance overflows
-// to +inf in FP32 and the other parameters' variances are unaffected.
-template <int NV>
-__device__ void mat_inv_diag(double (&M)[NV * NV], double (&diag)[NV]) {
-  for (int i = 0; i < NV; i++)
-    if (M[i * NV + i] == 0.0) M[i * NV + i] = 4.9406564584124654e-324;
-  double Minv[NV * NV];
-  for (int jj = 0; jj < NV; jj++) {
-    for (int ii = 1; ii <= jj; ii++) {
-      double t = 0.0;
-      for (int kk = 0; kk <= ii - 1; kk++) t += M[ii + kk * NV] * M[kk + jj * NV];
-      M[ii + jj * NV] -= t;
-    }
-    for (int ii = jj + 1; ii < NV; ii++) {
-      double t = 0.0;
-      for (int kk = 0; kk <= jj - 1; kk++) t += M[ii + kk * NV] * M[kk + jj * NV];
-      M[ii + jj * NV] = (1.0 / M[jj + jj * NV]) * (M[ii + jj * NV] - t);
-    }
+// ---------------------------------------------------------------------------
+// One ROI, one warp. The LM state is distributed over the lanes: lane l < NV
+// owns parameter l (value, previous value, sign, clamp), gradient entry l and
+// Hessian row l, so the small dense algebra of each step runs lane-parallel
+// with shuffles (a right-looking Cholesky, two triangular solves, one
+// refinement), and every per-parameter rule is one lane's instruction stream.
+// The decisions (convergence, accept / reject, damping) are warp-uniform.
+
+__device__ __forceinline__ float bcast(float v, int k) { return __shfl_sync(kFull, v, k); }
+
+// Initial clamp and fade of parameter l (CPUmleFit_LM.cpp:2434, :2786-2788,
+// :3191-3193).
+template <int MODE>
+__device__ __forceinline__ void clamp_fade(int l, float& c, float& f) {
+  if (MODE == 6) {
+    c = (l < 2) ? 2.0f : (l == 2) ? 10000.0f : 20.0f;
+    f = 0.5f;
+  } else if (MODE == 7) {
+    c = (l < 2) ? 1.0f : (l == 2) ? 10000.0f : (l == 3) ? 20.0f : (l == 4) ? 2.0f : 0.00001f;
+    f = (l < 2) ? 0.5f : (l == 2) ? 0.4f : (l == 3) ? 0.5f : (l == 4) ? 0.7f : 0.8f;
+  } else {
+    c = (l < 2) ? 1.0f : (l == 2) ? 10000.0f : (l == 3) ? 20.0f : (l < 7) ? 2.0f : 0.1f;
+    f = 0.5f;
   }
-  for (int num = 0; num < NV; num++) {
-    double yy[NV];
-    yy[0] = (num == 0) ? 1.0 : 0.0;
-    for (int ii = 1; ii < NV; ii++) {
-      double t = 0.0;
-      for (int jj = 0; jj <= ii - 1; jj++) t += M[ii + jj * NV] * yy[jj];
-      yy[ii] = ((ii == num) ? 1.0 : 0.0) - t;
-    }
-    Minv[NV - 1 + num * NV] = yy[NV - 1] / M[(NV - 1) + (NV - 1) * NV];
-    for (int ii = NV - 2; ii >= 0; ii--) {
-      double t = 0.0;
-      for (int jj = ii + 1; jj < NV; jj++) t += M[ii + jj * NV] * Minv[jj + num * NV];
-      Minv[ii + num * NV] = (1.0 / M[ii + ii * NV]) * (yy[ii] - t);
-    }
-  }
-  for (int i = 0; i < NV; i++) diag[i] = Minv[i * NV + i];
 }
 
-// ---------------------------------------------------------------------------
-// One ROI, one warp.
+// Lane-parallel solve of (L L^T) x = b: lane i holds b_i, row i of L (lr),
+// column i of L below the diagonal (lc[k] = L[k][i]) and 1 / L_ii.
+template <int NV>
+__device__ __forceinline__ float lane_solve(int lane, const float (&lr)[NV], const float (&lc)[NV],
+                                            float invd, float b) {
+  float y = b;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const float yk = bcast(y * invd, k);
+    if (lane == k) y = yk;
+    else if (lane > k) y = fmaf(-lr[k], yk, y);
+  }
+  float x = y;
+#pragma unroll
+  for (int k = NV - 1; k >= 0; --k) {
+    const float xk = bcast(x * invd, k);
+    if (lane == k) x = xk;
+    else if (lane < k) x = fmaf(-lc[k], xk, x);
+  }
+  return x;
+}
 
 template <int MODE>
 __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int lane, int64_t roi) {
@@ -647,9 +654,10 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   for (int p = lane; p < s2; p += 32) data[p] = __ldg(src + p);
   __syncwarp();
 
-  PHASE_BEGIN();
-  // Initial guesses (CPUgaussLib.cpp:172-225, CPUmleFit_LM.cpp:2477-2482).
-  float th[NV];
+  PHASE_DECL();
+  // Initial guesses (CPUgaussLib.cpp:172-225, CPUmleFit_LM.cpp:2477-2482),
+  // then lane l keeps parameter l.
+  float par;
   {
     FPair tx{0.f, 0.f}, ty{0.f, 0.f}, ts{0.f, 0.f};
     float mx = 0.0f, mn = 10e10f;
@@ -668,17 +676,14 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     tx = warp_sum_pair(tx);
     ty = warp_sum_pair(ty);
     ts = warp_sum_pair(ts);
-    float tsum = ts.hi + ts.lo;
-    th[0] = (tx.hi + tx.lo) / tsum;
-    th[1] = (ty.hi + ty.lo) / tsum;
+    const float tsum = ts.hi + ts.lo;
     if (__any_sync(kFull, nan_seen)) {
       // The reference's max/min fold is order dependent with NaN pixels:
       // replay it sequentially.
       mx = 0.0f;
       mn = 10e10f;
       for (int p0 = 0; p0 < s2; ++p0) {
-        int kk = p0 / s, ll = p0 - kk * s;
-        float d = data[kk * s + ll];
+        const float d = data[p0];
         mx = (mx > d) ? mx : d;
         mn = (mn < d) ? mn : d;
       }
@@ -691,56 +696,35 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     }
     // N0 = max(0, (max - min) * 2 * pi * 1.5 * 1.5), bg0 = max(min, 0.01),
     // evaluated in double as in the reference's expression.
-    double n0 = ((double)mx - (double)mn) * 2.0 * (double)3.141592f * 1.5 * 1.5;
-    th[2] = (float)((0.0 > n0) ? 0.0 : n0);
-    th[3] = (mn > 0.01f) ? mn : 0.01f;
+    const double n0 = ((double)mx - (double)mn) * 2.0 * (double)3.141592f * 1.5 * 1.5;
+    float v = 0.0f;
+    if (lane == 0) v = (tx.hi + tx.lo) / tsum;
+    if (lane == 1) v = (ty.hi + ty.lo) / tsum;
+    if (lane == 2) v = (float)((0.0 > n0) ? 0.0 : n0);
+    if (lane == 3) v = (mn > 0.01f) ? mn : 0.01f;
     if (MODE == 6) {
-      th[4] = (float)a.m.n[2] / 2.0f;
+      if (lane == 4) v = (float)a.m.n[2] / 2.0f;
     } else if (MODE == 7) {
-      if (a.m.init_p_len >= 2 && a.m.init_p[0] != 0.0f) {
-        th[4] = a.m.init_p[0];
-        th[5] = a.m.init_p[1];
-      } else {
-        th[4] = (float)a.m.n[2] / 2.0f;
-        th[5] = (float)a.m.n[3] / 2.0f;
-      }
+      const bool use = a.m.init_p_len >= 2 && a.m.init_p[0] != 0.0f;
+      if (lane == 4) v = use ? a.m.init_p[0] : (float)a.m.n[2] / 2.0f;
+      if (lane == 5) v = use ? a.m.init_p[1] : (float)a.m.n[3] / 2.0f;
     } else {
       // (z, w, u, g2) from initP, shared by all ROIs (CPUmleFit_LM.cpp:3246-3256)
-#pragma unroll
-      for (int i = 4; i < NV; ++i) th[i % NV] = a.m.init_p[(i - 4) & 3];
+      if (lane >= 4 && lane < 8) v = a.m.init_p[lane - 4];
     }
+    par = v;
   }
 
-  // LM state (CPUmleFit_LM.cpp:2425-2450).
-  float oth[NV], sign[NV], osign[NV], clampv[NV], oclamp[NV], fade[NV];
-#pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    oth[i] = th[i];
-    sign[i] = 0.0f;
-    osign[i] = 0.0f;
-  }
-  if (MODE == 6) {
-    const float c[5] = {2.0f, 2.0f, 10000.0f, 20.0f, 20.0f};
-#pragma unroll
-    for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = c[i % 5], fade[i] = 0.5f;
-  } else if (MODE == 7) {
-    const float c[6] = {1.0f, 1.0f, 10000.0f, 20.0f, 2.0f, 0.00001f};
-    const float fd[6] = {0.5f, 0.5f, 0.4f, 0.5f, 0.7f, 0.8f};
-#pragma unroll
-    for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = c[i % 6], fade[i] = fd[i % 6];
-  } else {
-    // CPUmleFit_LM.cpp:3191-3193
-    const float c[8] = {1.0f, 1.0f, 10000.0f, 20.0f, 2.0f, 2.0f, 2.0f, 0.1f};
-#pragma unroll
-    for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = c[i % 8], fade[i] = 0.5f;
-  }
-  float sum_update = 1e10f;
-  // Parameters of the last evaluation: fit type 8's CRLB pass reuses its
-  // positions, weights and g2 (CPUmleFit_LM.cpp:3568-3584).
-  float th_eval[NV];
-  float lambda = 1.0f, olambda = 1.0f;
+  // Per-lane LM state (CPUmleFit_LM.cpp:2425-2450): lane l < NV owns
+  // parameter l.
+  float opar = par, sg = 0.0f, osg = 0.0f, cl, fd, par_eval = par;
+  clamp_fade<MODE>(lane, cl, fd);
+  float ocl = cl;
+  float gl = 0.0f;   // gradient entry
+  float hr[NV];      // Hessian row, damped in place
+  // Warp-uniform state.
+  float lambda = 1.0f, olambda = 1.0f, sum_update = 1e10f;
   FPair err{1e12f, 0.0f}, oerr{1e13f, 0.0f};
-  float jac[NV], hes[NH];
   int turn = 1;
 
   // One evaluation call site for the initial pass, every accepted step and the
@@ -748,16 +732,19 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   int kk = 0;
   bool need_eval = true, first = true, fisher = false;
   FPair ll{0.0f, 0.0f};
+  float jac[NV], hes[NH];
   PHASE_MARK(5);
   for (;;) {
     if (need_eval) {
       FPair e;
+      // Parameters of the evaluation, broadcast to every lane. Fit type 8's
+      // CRLB pass keeps the positions and g2 of the last evaluation
+      // (CPUmleFit_LM.cpp:3568-3584) with the current N and bg.
+      if (!fisher) par_eval = par;
       float the[NV];
 #pragma unroll
-      for (int i = 0; i < NV; ++i) {
-        if (!fisher) th_eval[i] = th[i];
-        the[i] = (MODE == 8 && i != 2 && i != 3) ? th_eval[i] : th[i];
-      }
+      for (int k = 0; k < NV; ++k)
+        the[k] = bcast((MODE == 8 && fisher && k != 2 && k != 3) ? par_eval : par, k);
       evaluate<MODE>(a, L, ws, lane, the, first && MODE == 7, fisher, e, jac, hes);
       first = false;
       need_eval = false;
@@ -766,7 +753,20 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
         break;
       }
       err = e;
-      PHASE_BEGIN();
+      // this lane's gradient entry and Hessian row
+      gl = 0.0f;
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        if (lane == k) gl = jac[k];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        float v = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NV; ++i)
+          if (lane == i) v = hes[hidx<NV>(i < k ? i : k, i < k ? k : i)];
+        hr[k] = v;
+      }
+      PHASE_RESET();
     }
     if (kk >= a.iterations) {
       fisher = true;
@@ -778,9 +778,9 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
                      : nullptr;
     // |(newErr - oldErr) / newErr| < 1e-6 (CPUmleFit_LM.cpp:2565)
     {
-      float dhi = err.hi - oerr.hi;
-      float dlo = err.lo - oerr.lo;
-      float rel = fabsf((dhi + dlo) / (err.hi + err.lo));
+      const float dhi = err.hi - oerr.hi;
+      const float dlo = err.lo - oerr.lo;
+      const float rel = fabsf((dhi + dlo) / (err.hi + err.lo));
       if (rec) {
         rec[0] = (float)kk;
         rec[1] = rel;
@@ -799,12 +799,9 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     // newErr > 1.5 * oldErr, evaluated in double by the reference: the FMA
     // forms 1.5 * oldErr - newErr with one rounding, which keeps its sign.
     if (fmaf(1.5f, e_old, -e_new) < 0.0f) {
-#pragma unroll
-      for (int i = 0; i < NV; i++) {
-        sign[i] = osign[i];
-        clampv[i] = oclamp[i];
-        th[i] = oth[i];
-      }
+      sg = osg;
+      cl = ocl;
+      par = opar;
       lambda = olambda;
       err = oerr;
       lambda = 10.0f * lambda;
@@ -814,15 +811,11 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
       else if (lambda < 1.0f)
         lambda = 1.0f;
     }
-    // H_ii *= lambda, in place (cumulative across failed solves, as in the
+    // H_ll *= lambda, in place (cumulative across failed solves, as in the
     // reference).
 #pragma unroll
-    for (int i = 0; i < NV; i++) hes[hidx<NV>(i, i)] *= lambda;
-    float full[NV * NV], u[NV * NV], upd[NV], rhs[NV];
-#pragma unroll
-    for (int l = 0; l < NV; ++l)
-#pragma unroll
-      for (int mm = l; mm < NV; ++mm) full[l * NV + mm] = full[mm * NV + l] = hes[hidx<NV>(l, mm)];
+    for (int k = 0; k < NV; ++k)
+      if (lane == k) hr[k] *= lambda;
     // A parameter whose derivative is exactly zero at every pixel (z on the
     // mirror-padded boundary knot) has an exactly zero Hessian row. The
     // reference only survives that case through rounding noise of its double
@@ -830,163 +823,237 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     // sign, cut to +-clamp); an exact zero would give NaN. Such a parameter is
     // held for this step instead: its row becomes the identity and its
     // gradient zero.
+    bool frz = false;
 #pragma unroll
-    for (int l = 0; l < NV; ++l) {
-      rhs[l] = jac[l];
-      if (full[l * NV + l] == 0.0f) {
+    for (int k = 0; k < NV; ++k)
+      if (lane == k) frz = (hr[k] == 0.0f);
+    const unsigned fmask = __ballot_sync(kFull, frz && lane < NV);
+    float am[NV], ar[NV];
 #pragma unroll
-        for (int mm = 0; mm < NV; ++mm) full[l * NV + mm] = full[mm * NV + l] = 0.0f;
-        full[l * NV + l] = 1.0f;
-        rhs[l] = 0.0f;
+    for (int k = 0; k < NV; ++k) {
+      am[k] = ((fmask >> k) & 1u) ? 0.0f : hr[k];
+      if (frz) am[k] = (k == lane) ? 1.0f : 0.0f;
+      ar[k] = am[k];
+    }
+    const float rhs = frz ? 0.0f : gl;
+    // Right-looking Cholesky (CPUsplineLib.cpp:1363-1390 computes the same
+    // factor; it fails on a negative pivot only).
+    float lr[NV], lc[NV], invd = 1.0f;
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      lr[j] = 0.0f;
+      lc[j] = 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      const float ajj = bcast(am[j], j);
+      if (!(ajj >= 0.0f)) {
+        ok = false;
+        break;
+      }
+      const float ljj = sqrtf(ajj);
+      const float inv = 1.0f / ljj;
+      const float lij = (lane > j) ? am[j] * inv : ((lane == j) ? ljj : 0.0f);
+      lr[j] = lij;
+      if (lane == j) invd = inv;
+#pragma unroll
+      for (int k = j + 1; k < NV; ++k) {
+        const float lkj = bcast(lij, k);
+        if (lane == j) lc[k] = lkj;
+        if (lane > j && k <= lane) am[k] = fmaf(-lij, lkj, am[k]);
       }
     }
-    bool ok = cholesky<NV>(full, u);
-    if (ok && (a.flags & FLAG_NO_REFINE)) {
-      chol_solve<NV>(u, rhs, upd);
-      if (MODE != 6) {
-        bool bad = false;
+    float upd = 0.0f;
+    if (ok) {
+      upd = lane_solve<NV>(lane, lr, lc, invd, rhs);
+      if (!(a.flags & FLAG_NO_REFINE)) {
+        // One refinement step: r = b - A upd with error-free products.
+        float sh = rhs, sl = 0.0f;
 #pragma unroll
-        for (int i = 0; i < NV; ++i) bad |= (upd[i] != upd[i]);
-        if (bad) ok = false;
-      }
-    } else if (ok) {
-      chol_solve<NV>(u, rhs, upd);
-      // One refinement step: r = J - H upd with error-free products.
-      float r[NV];
-#pragma unroll
-      for (int i = 0; i < NV; ++i) {
-        float sh = rhs[i], sl = 0.0f;
-#pragma unroll
-        for (int j = 0; j < NV; ++j) {
-          float p, pe, t, te;
-          two_prod(full[i * NV + j], upd[j], p, pe);
-          two_sum(sh, -p, t, te);
-          sh = t;
-          sl += te - pe;
+        for (int k = 0; k < NV; ++k) {
+          const float xk = bcast(upd, k);
+          float p_, pe_, t_, te_;
+          two_prod(ar[k], xk, p_, pe_);
+          two_sum(sh, -p_, t_, te_);
+          sh = t_;
+          sl += te_ - pe_;
         }
-        r[i] = sh + sl;
+        upd += lane_solve<NV>(lane, lr, lc, invd, sh + sl);
       }
-      float corr[NV];
-      chol_solve<NV>(u, r, corr);
-#pragma unroll
-      for (int i = 0; i < NV; ++i) upd[i] += corr[i];
       if (MODE != 6) {
-        bool bad = false;
-#pragma unroll
-        for (int i = 0; i < NV; ++i) bad |= (upd[i] != upd[i]);
-        if (bad) ok = false;  // CPUmleFit_LM.cpp:2943-2950
+        // CPUmleFit_LM.cpp:2943-2950: a NaN step counts as a failed solve
+        if (__any_sync(kFull, lane < NV && upd != upd)) ok = false;
       }
     }
     if (ok) {
-      if (MODE == 7) upd[5] = upd[5] * 10.0f;  // :2951
-#pragma unroll
-      for (int i = 0; i < NV; i++) {
-        osign[i] = sign[i];
-        oclamp[i] = clampv[i];
-        oth[i] = th[i];
-      }
+      if (MODE == 7 && lane == 5) upd = upd * 10.0f;  // :2951
+      osg = sg;
+      ocl = cl;
+      opar = par;
       olambda = lambda;
       oerr = err;
       if (MODE == 7) {
         // "let it go" (:2966-2971)
-        if (fabsf(upd[4]) < 0.005f && turn) {
-          clampv[5] = (float)a.m.n[3] / 10.0f;
-          oclamp[5] = clampv[5];
+        const float dz = bcast(upd, 4);
+        if (fabsf(dz) < 0.005f && turn) {
+          if (lane == 5) cl = ocl = (float)a.m.n[3] / 10.0f;
+          if (lane == 4) cl = ocl = 2.0f;
           turn = 0;
-          clampv[4] = 2.0f;
-          oclamp[4] = 2.0f;
         }
       }
-      if (MODE == 8) sum_update = 0.0f;
-#pragma unroll
-      for (int l = 0; l < NV; l++) {
-        if (sign[l] != 0.0f) {
-          if ((sign[l] == 1.0f && upd[l] < 0.0f) || (sign[l] == -1.0f && upd[l] > 0.0f))
-            clampv[l] = clampv[l] * fade[l];
-        }
-        sign[l] = (upd[l] > 0.0f) ? 1.0f : -1.0f;
-        const float step = upd[l] / (1.0f + fabsf(upd[l] / clampv[l]));
-        th[l] = th[l] - step;
-        if (MODE == 8) sum_update += fabsf(step);
+      if (sg != 0.0f) {
+        if ((sg == 1.0f && upd < 0.0f) || (sg == -1.0f && upd > 0.0f)) cl = cl * fd;
+      }
+      sg = (upd > 0.0f) ? 1.0f : -1.0f;
+      const float step = upd / (1.0f + fabsf(upd / cl));
+      par = par - step;
+      if (MODE == 8) sum_update = warp_sum(lane < NV ? fabsf(step) : 0.0f);
+      // Bounds (CPUmleFit_LM.cpp:2626-2634, :3003-3010, :3421-3447).
+      if (MODE == 8 && lane < 2) {
+        const float lo = (float)(s - 1) / 2.0f - (float)s / 4.0f;  // exact for s <= 51
+        const float hi = (float)(s - 1) / 2.0f + (float)s / 4.0f;
+        par = (par > lo) ? par : lo;
+        par = (par < hi) ? par : hi;
+      }
+      if (lane == 2) par = (par > 1.0f) ? par : 1.0f;
+      // max(bg, 0.01) in double: no float lies strictly between 0.01f and
+      // 0.01, so the float comparison selects the same branch.
+      if (lane == 3) par = (par > 0.01f) ? par : 0.01f;
+      if (lane == 4) {
+        par = (par > 0.0f) ? par : 0.0f;
+        const float zmax = (MODE == 6) ? (float)(a.m.n[2] - 4) : (float)a.m.n[2] - 0.5f;
+        par = (par < zmax) ? par : zmax;
+      }
+      if (MODE == 7 && lane == 5) {
+        par = (par > 0.0f) ? par : 0.0f;
+        const float wmax = (float)a.m.n[3] - 0.5f;
+        par = (par < wmax) ? par : wmax;
       }
       if (MODE == 8) {
-        // x, y within (s-1)/2 +- s/4 (exact in float for s <= 51), CPUmleFit_LM.cpp:3421-3424
-        const float lo = (float)(s - 1) / 2.0f - (float)s / 4.0f;
-        const float hi = (float)(s - 1) / 2.0f + (float)s / 4.0f;
-        th[0] = (th[0] > lo) ? th[0] : lo;
-        th[0] = (th[0] < hi) ? th[0] : hi;
-        th[1] = (th[1] > lo) ? th[1] : lo;
-        th[1] = (th[1] < hi) ? th[1] : hi;
-      }
-      th[2] = (th[2] > 1.0f) ? th[2] : 1.0f;
-      // max(bg, 0.01) in double: no float lies strictly between 0.01f and 0.01,
-      // so the float comparison selects the same branch.
-      th[3] = (th[3] > 0.01f) ? th[3] : 0.01f;
-      th[4] = (th[4] > 0.0f) ? th[4] : 0.0f;
-      if (MODE == 6) {
-        float zmax = (float)(a.m.n[2] - 4);
-        th[4] = (th[4] < zmax) ? th[4] : zmax;
-      } else if (MODE == 7) {
-        const float zmax = (float)a.m.n[2] - 0.5f;  // exact: n - 0.5 is a float
-        th[4] = (th[4] < zmax) ? th[4] : zmax;
-        th[5] = (th[5] > 0.0f) ? th[5] : 0.0f;
-        const float wmax = (float)a.m.n[3] - 0.5f;
-        th[5] = (th[5] < wmax) ? th[5] : wmax;
-      } else {
-        const float zmax = (float)a.m.n[2] - 0.5f;
-        th[4] = (th[4] < zmax) ? th[4] : zmax;
-        // periodic azimuth (CPUmleFit_LM.cpp:3436-3443): period nW - 2
-        const int nw = a.m.n[3];
-        if (th[5] <= 1.0f)
-          th[5] = (float)(nw - 2) + th[5];
-        else if (th[5] > (float)(nw - 1))
-          th[5] = (2.0f + th[5]) - (float)nw;
-        th[6] = (th[6] > 1.0f) ? th[6] : 1.0f;
-        const float umax = (float)a.m.n[4] - 0.5f;
-        th[6] = (th[6] < umax) ? th[6] : umax;
-        th[7 % NV] = (th[7 % NV] < 1.0f) ? th[7 % NV] : 1.0f;
-        th[7 % NV] = (th[7 % NV] > 0.0f) ? th[7 % NV] : 0.0f;
+        if (lane == 5) {
+          // periodic azimuth (:3436-3443): period nW - 2
+          const int nw = a.m.n[3];
+          if (par <= 1.0f)
+            par = (float)(nw - 2) + par;
+          else if (par > (float)(nw - 1))
+            par = (2.0f + par) - (float)nw;
+        }
+        if (lane == 6) {
+          par = (par > 1.0f) ? par : 1.0f;
+          const float umax = (float)a.m.n[4] - 0.5f;
+          par = (par < umax) ? par : umax;
+        }
+        if (lane == 7) {
+          par = (par < 1.0f) ? par : 1.0f;
+          par = (par > 0.0f) ? par : 0.0f;
+        }
       }
       need_eval = true;
     } else {
       lambda = 10.0f * lambda;
     }
-    if (rec) {
-      const float e_n = 0.0f;  // deviance after the step: next record's [2]
-      rec[4] = (e_new > 1.5f * e_old ? 2.0f : 0.0f) + (e_new < e_old ? 4.0f : 0.0f) + (ok ? 8.0f : 0.0f);
-      rec[5] = lambda;
+    if (a.trace) {
+      // decision record (diagnostics): gathered from the parameter lanes
 #pragma unroll
-      for (int i = 0; i < NV; ++i) rec[6 + i] = ok ? upd[i] : 0.0f;
-#pragma unroll
-      for (int i = 0; i < NV; ++i) rec[14 + i] = th[i];
-      rec[22] = e_n;
+      for (int k = 0; k < NV; ++k) {
+        const float uk = bcast(ok ? upd : 0.0f, k);
+        const float pk = bcast(par, k);
+        if (rec) {
+          rec[6 + k] = uk;
+          rec[14 + k] = pk;
+        }
+      }
+      if (rec) {
+        rec[4] = (e_new > 1.5f * e_old ? 2.0f : 0.0f) + (e_new < e_old ? 4.0f : 0.0f) + (ok ? 8.0f : 0.0f);
+        rec[5] = lambda;
+        rec[22] = 0.0f;
+      }
     }
     ++kk;
     PHASE_MARK(6);
   }
 
-  // CRLB and log-likelihood at the final theta (the Fisher pass above).
-  float* fm = hes;
-  double M[NV * NV], diag[NV];
-#pragma unroll
-  for (int l = 0; l < NV; ++l)
-#pragma unroll
-    for (int mm = l; mm < NV; ++mm) M[l * NV + mm] = M[mm * NV + l] = (double)fm[hidx<NV>(l, mm)];
+  // CRLB = diag(M^-1) of the Fisher matrix M (the reference inverts it with an
+  // unpivoted LU, VC/CPUmleFit_LM/MatInvLib.h:17-77). Here, lane-parallel in
+  // FP32 on the Jacobi-scaled matrix S = D^-1 M D^-1 (unit diagonal, so its
+  // condition number is that of the parameters' correlations, not of their
+  // units): Cholesky S = L L^T, then diag(S^-1)_c = sum_k ((L^-1)_kc)^2 with the
+  // columns of L^-1 by forward substitution, and (M^-1)_cc = (S^-1)_cc / M_cc.
+  // A parameter with an exactly zero Fisher row (zero derivative everywhere)
+  // is decoupled: its variance is +inf, the others are unaffected.
+  PHASE_RESET();
+  float crlb = 0.0f;  // lane c: variance of parameter c
   {
-    PHASE_BEGIN();
-    mat_inv_diag<NV>(M, diag);
-    PHASE_MARK(7);
+    float mr[NV], dk[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) dk[k] = hes[hidx<NV>(k, k)];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      float v = 0.0f;
+#pragma unroll
+      for (int i = 0; i < NV; ++i)
+        if (lane == i) {
+          const float mik = hes[hidx<NV>(i < k ? i : k, i < k ? k : i)];
+          const float den = sqrtf(dk[i]) * sqrtf(dk[k]);
+          v = (i == k) ? 1.0f : ((den > 0.0f) ? mik / den : 0.0f);
+        }
+      mr[k] = v;
+    }
+    float lr[NV], invd = 1.0f;
+    bool okc = true;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) lr[j] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      const float ajj = bcast(mr[j], j);
+      if (!(ajj > 0.0f)) okc = false;
+      const float ljj = sqrtf(ajj);
+      const float inv = 1.0f / ljj;
+      const float lij = (lane > j) ? mr[j] * inv : ((lane == j) ? ljj : 0.0f);
+      lr[j] = lij;
+      if (lane == j) invd = inv;
+#pragma unroll
+      for (int k = j + 1; k < NV; ++k) {
+        const float lkj = bcast(lij, k);
+        if (lane > j && k <= lane) mr[k] = fmaf(-lij, lkj, mr[k]);
+      }
+    }
+    // columns of L^-1: z = L^-1 e_c, lane i holds z_i; accumulate z_i^2 per c
+    float acc[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+      float part = 0.0f, z = 0.0f;
+#pragma unroll
+      for (int k = c; k < NV; ++k) {
+        const float zk = bcast(((k == c ? 1.0f : 0.0f) - part) * invd, k);
+        if (lane == k) z = zk;
+        else if (lane > k) part = fmaf(lr[k], zk, part);
+      }
+      acc[c] = (lane >= c && lane < NV) ? z * z : 0.0f;
+    }
+    warp_sum_array<NV>(acc);
+#pragma unroll
+    for (int c = 0; c < NV; ++c)
+      if (lane == c) crlb = okc ? acc[c] / dk[c] : __int_as_float(0x7fc00000);
+    // decoupled zero rows
+#pragma unroll
+    for (int c = 0; c < NV; ++c)
+      if (lane == c && dk[c] == 0.0f) crlb = __int_as_float(0x7f800000);
   }
+  PHASE_MARK(7);
+  float thv[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) thv[k] = bcast(par, k);
   if (lane == 0) {
     const int64_t n = a.out_n;
     const int64_t o = a.out_offset + roi;
 #pragma unroll
-    for (int i = 0; i < NV; ++i) a.P[i * n + o] = th[i];
+    for (int i = 0; i < NV; ++i) a.P[i * n + o] = thv[i];
     a.P[NV * n + o] = (float)kk;
-#pragma unroll
-    for (int i = 0; i < NV; ++i) a.CRLB[i * n + o] = (float)diag[i];
     a.LL[o] = ll.hi + ll.lo;
   }
+  if (lane < NV) a.CRLB[lane * a.out_n + a.out_offset + roi] = crlb;
   __syncwarp();
 }
 

@@ -91,6 +91,23 @@ __device__ __forceinline__ void warp_sum_array(float (&v)[K]) {
   }
 }
 
+// Reduce-scatter of 32 values over the warp: each lane passes in its 32
+// partial values and gets back the warp total of value number `lane`. Five
+// exchange levels, 31 shuffles (an all-reduce of the same values takes 160).
+__device__ __forceinline__ float reduce_scatter32(float (&v)[32], int lane) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < o; ++i) {
+      const float send = up ? v[i] : v[i + o];
+      const float keep = up ? v[i + o] : v[i];
+      v[i] = keep + __shfl_xor_sync(kFull, send, o);
+    }
+  }
+  return v[0];
+}
+
 // Error-free transformations (Knuth two-sum, FMA two-product).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;

@@ -39,7 +39,7 @@
 // Minimum resident blocks per SM requested for the 3D kernels (4 warps each):
 // trades registers for occupancy.
 #ifndef BSFIT_MINBLOCKS6
-#define BSFIT_MINBLOCKS6 4
+#define BSFIT_MINBLOCKS6 5
 #endif
 
 namespace bsfit {
@@ -136,6 +136,13 @@ struct Eval {
   static constexpr int NH = NV * (NV + 1) / 2;
 };
 
+// index of (l, m), l <= m, in the packed upper triangle of an NV x NV matrix
+template <int NV>
+__device__ __forceinline__ int hidx(int l, int m) {
+  // index of (l, m), l <= m, in the packed upper triangle
+  return l * NV - (l * (l - 1)) / 2 + (m - l);
+}
+
 // Row/column of item t of a row-major (rows x w) grid for a lane that starts at
 // t = lane and advances by 32: avoids a runtime integer division per item.
 struct Stride2D {
@@ -156,11 +163,12 @@ struct Stride2D {
   }
 };
 
+// Outputs are distributed over the lanes: lane l < NV receives gradient entry
+// l (gl) and Hessian row l (hr), or Fisher row l; err_out is on every lane.
 template <int MODE>
 __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int lane,
-                         const float* th, bool dup45, bool FISHER, FPair& err_out,
-                         float (&jac)[ModeTraits<MODE>::NV],
-                         float (&hes)[ModeTraits<MODE>::NV * (ModeTraits<MODE>::NV + 1) / 2]) {
+                         const float* th, bool dup45, bool FISHER, FPair& err_out, float& gl,
+                         float (&hr)[ModeTraits<MODE>::NV]) {
   using TR = ModeTraits<MODE>;
   constexpr int D = TR::D;
   constexpr int NV = TR::NV;
@@ -420,12 +428,15 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
   __syncwarp();
   PHASE_MARK(2);
 
-  // (C) X contraction per pixel, fused with the likelihood sums.
+  // (C) X contraction per pixel, fused with the likelihood sums. acc holds
+  // this lane's partial gradient (0 .. NV-1) and packed Hessian or Fisher
+  // upper triangle (NV .. NV+NH-1).
+  constexpr int K = NV + NH;
+  constexpr int KP = (K + 31) / 32 * 32;
   FPair err{0.0f, 0.0f};
+  float acc[KP];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) jac[k] = 0.0f;
-#pragma unroll
-  for (int k = 0; k < NH; ++k) hes[k] = 0.0f;
+  for (int k = 0; k < KP; ++k) acc[k] = 0.0f;
   {
     const float bx0 = w[8], bx1 = w[9], bx2 = w[10], bx3 = w[11];
     const float dx0 = w[12], dx1 = w[13], dx2 = w[14];
@@ -509,23 +520,23 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
         const float t1 = 1.0f - dm;
         const float t2 = dm * inv;
 #pragma unroll
-        for (int l = 0; l < NV; ++l) jac[l] = fmaf(t1, dudt[l], jac[l]);
-        int k = 0;
+        for (int l = 0; l < NV; ++l) acc[l] = fmaf(t1, dudt[l], acc[l]);
+        int k = NV;
 #pragma unroll
         for (int l = 0; l < NV; ++l) {
           const float tl = t2 * dudt[l];
 #pragma unroll
-          for (int mm = l; mm < NV; ++mm, ++k) hes[k] = fmaf(tl, dudt[mm], hes[k]);
+          for (int mm = l; mm < NV; ++mm, ++k) acc[k] = fmaf(tl, dudt[mm], acc[k]);
         }
       } else {
         // Fisher information and log-likelihood (CPUmleFit_LM.cpp:2730-2742).
         const float im = inv;
-        int k = 0;
+        int k = NV;
 #pragma unroll
         for (int l = 0; l < NV; ++l) {
           const float tl = dudt[l] * im;
 #pragma unroll
-          for (int mm = l; mm < NV; ++mm, ++k) hes[k] = fmaf(tl, dudt[mm], hes[k]);
+          for (int mm = l; mm < NV; ++mm, ++k) acc[k] = fmaf(tl, dudt[mm], acc[k]);
         }
         if (model > 0.0f) {
           float ll = (d > 0.0f) ? (d * logf(model) - model - d * logf(d) + d) : -model;
@@ -535,8 +546,31 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
     }
   }
   PHASE_MARK(3);
-  warp_sum_array<NV>(jac);
-  warp_sum_array<NH>(hes);
+  // Reduce-scatter: lane t gets the total of value t (and t + 32).
+  float t0, t1 = 0.0f;
+  {
+    float v[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = acc[k];
+    t0 = reduce_scatter32(v, lane);
+  }
+  if constexpr (KP > 32) {
+    float v[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = acc[32 + (k % (KP - 32))];
+#pragma unroll
+    for (int k = KP - 32; k < 32; ++k) v[k] = 0.0f;
+    t1 = reduce_scatter32(v, lane);
+  }
+  gl = t0;  // value index l = gradient entry l on lane l
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const int lo = lane < k ? lane : k, hi = lane < k ? k : lane;
+    const int idx = (lane < NV) ? NV + hidx<NV>(lo, hi) : 0;
+    const float a0 = __shfl_sync(kFull, t0, idx & 31);
+    const float a1 = (KP > 32) ? __shfl_sync(kFull, t1, idx & 31) : 0.0f;
+    hr[k] = (idx < 32) ? a0 : a1;
+  }
   err_out = warp_sum_pair(err);
   PHASE_MARK(4);
 }
@@ -544,11 +578,6 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
 // ---------------------------------------------------------------------------
 // LM helpers (warp-uniform register state).
 
-template <int NV>
-__device__ __forceinline__ int hidx(int l, int m) {
-  // index of (l, m), l <= m, in the packed upper triangle
-  return l * NV - (l * (l - 1)) / 2 + (m - l);
-}
 
 // Unpivoted Cholesky of the full matrix a (row-major NV x NV), lower factor in
 // u (u[i*NV + j], j <= i). Fails on a negative pivot only
@@ -721,7 +750,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   clamp_fade<MODE>(lane, cl, fd);
   float ocl = cl;
   float gl = 0.0f;   // gradient entry
-  float hr[NV];      // Hessian row, damped in place
+  float hr[NV];      // Hessian row (damped in place), or the Fisher row
   // Warp-uniform state.
   float lambda = 1.0f, olambda = 1.0f, sum_update = 1e10f;
   FPair err{1e12f, 0.0f}, oerr{1e13f, 0.0f};
@@ -732,7 +761,6 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   int kk = 0;
   bool need_eval = true, first = true, fisher = false;
   FPair ll{0.0f, 0.0f};
-  float jac[NV], hes[NH];
   PHASE_MARK(5);
   for (;;) {
     if (need_eval) {
@@ -745,7 +773,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
 #pragma unroll
       for (int k = 0; k < NV; ++k)
         the[k] = bcast((MODE == 8 && fisher && k != 2 && k != 3) ? par_eval : par, k);
-      evaluate<MODE>(a, L, ws, lane, the, first && MODE == 7, fisher, e, jac, hes);
+      evaluate<MODE>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr);
       first = false;
       need_eval = false;
       if (fisher) {
@@ -753,19 +781,6 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
         break;
       }
       err = e;
-      // this lane's gradient entry and Hessian row
-      gl = 0.0f;
-#pragma unroll
-      for (int k = 0; k < NV; ++k)
-        if (lane == k) gl = jac[k];
-#pragma unroll
-      for (int k = 0; k < NV; ++k) {
-        float v = 0.0f;
-#pragma unroll
-        for (int i = 0; i < NV; ++i)
-          if (lane == i) v = hes[hidx<NV>(i < k ? i : k, i < k ? k : i)];
-        hr[k] = v;
-      }
       PHASE_RESET();
     }
     if (kk >= a.iterations) {
@@ -986,19 +1001,17 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
   float crlb = 0.0f;  // lane c: variance of parameter c
   {
     float mr[NV], dk[NV];
+    float mydiag = 0.0f;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) dk[k] = hes[hidx<NV>(k, k)];
+    for (int k = 0; k < NV; ++k)
+      if (lane == k) mydiag = hr[k];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) dk[k] = bcast(mydiag, k);
+    const float sd = sqrtf(mydiag);
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      float v = 0.0f;
-#pragma unroll
-      for (int i = 0; i < NV; ++i)
-        if (lane == i) {
-          const float mik = hes[hidx<NV>(i < k ? i : k, i < k ? k : i)];
-          const float den = sqrtf(dk[i]) * sqrtf(dk[k]);
-          v = (i == k) ? 1.0f : ((den > 0.0f) ? mik / den : 0.0f);
-        }
-      mr[k] = v;
+      const float den = sd * sqrtf(dk[k]);
+      mr[k] = (lane == k) ? 1.0f : ((den > 0.0f) ? hr[k] / den : 0.0f);
     }
     float lr[NV], invd = 1.0f;
     bool okc = true;
@@ -1176,15 +1189,15 @@ __global__ void __launch_bounds__(128) eval_kernel(FitArgs a, const float* theta
 #pragma unroll
     for (int i = 0; i < NV; ++i) th[i] = theta[i * a.nfits + roi];
     FPair e;
-    float jac[NV], hes[NH];
-    evaluate<MODE>(a, L, ws, lane, th, false, fisher != 0, e, jac, hes);
-    if (lane == 0) {
-      float* o = out + roi * (1 + NV + NH);
-      o[0] = e.hi + e.lo;
+    float gl, hr[NV];
+    evaluate<MODE>(a, L, ws, lane, th, false, fisher != 0, e, gl, hr);
+    float* o = out + roi * (1 + NV + NH);
+    if (lane == 0) o[0] = e.hi + e.lo;
+    if (lane < NV) {
+      o[1 + lane] = fisher ? 0.0f : gl;
 #pragma unroll
-      for (int i = 0; i < NV; ++i) o[1 + i] = fisher ? 0.0f : jac[i];
-#pragma unroll
-      for (int i = 0; i < NH; ++i) o[1 + NV + i] = hes[i];
+      for (int k = 0; k < NV; ++k)
+        if (k >= lane) o[1 + NV + hidx<NV>(lane, k)] = hr[k];
     }
     __syncwarp();
   }

@@ -189,6 +189,93 @@ class Batch:
         return c[:k].copy(), c[k:2 * k].copy()
 
 
+class Server:
+    """Continuous-batching request loop (bsfit_server_*).
+
+    submit([(model, rois, iterations), ...]) stages the ROIs in page-locked
+    host memory, returns a request id and queues or starts the request;
+    poll() returns {id: [(P, CRLB, LL), ...]} for every request finished since
+    the last call (P (N, NV+1), CRLB (N, NV), LL (N,) per segment, as
+    GPUmleFit_LM_multiD); wait(id) blocks until one request is done."""
+
+    def __init__(self, max_inflight=4, arena_bytes=2 << 30):
+        h = np.ctypeslib.ctypes.c_void_p()
+        check(_native.lib().bsfit_server_create(int(max_inflight), int(arena_bytes),
+                                                np.ctypeslib.ctypes.byref(h)), "bsfit_server_create")
+        self._h = h
+        self._live = {}
+
+    def submit(self, entries):
+        import torch
+        segs = (_native.HostSegment * len(entries))()
+        keep = []
+        for k, (m, rois, it) in enumerate(entries):
+            r = torch.as_tensor(np.ascontiguousarray(rois, dtype=np.float32))
+            if r.ndim == 2:
+                r = r[None]
+            r = r.pin_memory()
+            n, s = r.shape[0], r.shape[-1]
+            P = torch.empty((m.nv + 1, n), dtype=torch.float32).pin_memory()
+            C = torch.empty((m.nv, n), dtype=torch.float32).pin_memory()
+            L = torch.empty((n,), dtype=torch.float32).pin_memory()
+            keep.append((m, r, P, C, L))
+            segs[k].model = m._h.value
+            segs[k].rois = r.data_ptr()
+            segs[k].roi_size = s
+            segs[k].nfits = n
+            segs[k].iterations = int(it)
+            segs[k].P, segs[k].CRLB, segs[k].LL = P.data_ptr(), C.data_ptr(), L.data_ptr()
+        rid = np.ctypeslib.ctypes.c_int64()
+        check(_native.lib().bsfit_server_submit(self._h, np.ctypeslib.ctypes.cast(segs, np.ctypeslib.ctypes.c_void_p),
+                                                len(entries), np.ctypeslib.ctypes.byref(rid)),
+              "bsfit_server_submit")
+        self._live[rid.value] = (segs, keep)
+        return rid.value
+
+    def _results(self, rid):
+        segs, keep = self._live.pop(rid)
+        return [(P.numpy().T.copy(), C.numpy().T.copy(), L.numpy().copy()) for m, r, P, C, L in keep]
+
+    def poll(self):
+        ct = np.ctypeslib.ctypes
+        ids = (ct.c_int64 * 256)()
+        n = ct.c_int32()
+        out = {}
+        while True:
+            check(_native.lib().bsfit_server_poll(self._h, ids, 256, ct.byref(n)), "bsfit_server_poll")
+            for i in range(n.value):
+                out[ids[i]] = self._results(ids[i])
+            if n.value < 256:
+                return out
+
+    def wait(self, rid, timeout=60.0):
+        check(_native.lib().bsfit_server_wait(self._h, int(rid), float(timeout)), "bsfit_server_wait")
+        return self._results(rid)
+
+    def stats(self):
+        ct = np.ctypeslib.ctypes
+        d = [ct.c_double() for _ in range(3)]
+        i = [ct.c_int64() for _ in range(3)]
+        check(_native.lib().bsfit_server_stats(self._h, *[ct.byref(x) for x in d],
+                                               *[ct.byref(x) for x in i]), "bsfit_server_stats")
+        return {"p50_ms": d[0].value, "p99_ms": d[1].value, "fits_per_s": d[2].value,
+                "completed": i[0].value, "in_flight": i[1].value, "queued": i[2].value}
+
+    def reset_stats(self):
+        check(_native.lib().bsfit_server_reset_stats(self._h), "bsfit_server_reset_stats")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.lib().bsfit_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def measure_fp32_peak():
     """Measured FP32 FMA throughput of the current device, TFLOP/s."""
     v = np.ctypeslib.ctypes.c_double()

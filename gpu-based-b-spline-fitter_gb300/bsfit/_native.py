@@ -37,6 +37,18 @@ SIGNATURES = {
     "bsfit_batch_fit_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "bsfit_batch_fit_device_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "bsfit_model_fittype": (ctypes.c_int32, [ctypes.c_void_p]),
+    "bsfit_server_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "bsfit_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "bsfit_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                           ctypes.POINTER(ctypes.c_int64)]),
+    "bsfit_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                         ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+    "bsfit_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double]),
+    "bsfit_server_stats": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_double)] * 3 +
+                           [ctypes.POINTER(ctypes.c_int64)] * 3),
+    "bsfit_server_reset_stats": (ctypes.c_int, [ctypes.c_void_p]),
     "bsfit_fit_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -76,3 +88,11 @@ class Segment(ctypes.Structure):
                 ("roi_size", ctypes.c_int64), ("nfits", ctypes.c_int64),
                 ("iterations", ctypes.c_int32), ("d_P", ctypes.c_void_p),
                 ("d_CRLB", ctypes.c_void_p), ("d_LL", ctypes.c_void_p)]
+
+
+class HostSegment(ctypes.Structure):
+    """bsfit_host_segment (include/bsfit.h)."""
+    _fields_ = [("model", ctypes.c_void_p), ("rois", ctypes.c_void_p),
+                ("roi_size", ctypes.c_int64), ("nfits", ctypes.c_int64),
+                ("iterations", ctypes.c_int32), ("P", ctypes.c_void_p),
+                ("CRLB", ctypes.c_void_p), ("LL", ctypes.c_void_p)]

@@ -160,6 +160,8 @@ int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
   return BSFIT_OK;
 }
 
+int32_t bsfit_model_fittype(bsfit_model model) { return model ? model->dev.fittype : 0; }
+
 int bsfit_model_release(bsfit_model model) {
   if (!model) return BSFIT_E_INVALID;
   cudaFree(model->d_coeff);

@@ -1,0 +1,393 @@
+// Serving form: a continuous-batching request loop over the batched fitter.
+//
+// The reference's GUI fits blocks of ROIs synchronously, one mex call at a time
+// (MultiD_fitter/simplefitter_cspline.m:309-313, 463-524). Here requests (the
+// ROI batches of acquired frames, each with its own PSF model) are submitted
+// while others run:
+//  - a fixed pool of slots, one CUDA stream each, bounds the requests in flight;
+//  - device memory for ROIs, results and work-queue counters comes from one
+//    arena reserved when the server is created (the HBM budget); a request is
+//    admitted when a slot and enough arena space are free, otherwise it waits
+//    in submission order;
+//  - an admitted request runs host-to-device copies, one persistent batched
+//    launch and device-to-host copies on its slot's stream, so requests in
+//    flight overlap on the GPU (a new request's blocks start as the running
+//    ones retire);
+//  - a host callback at the end of the stream marks the request done with its
+//    completion time, so results are returned per request as soon as they are
+//    ready and the latency (submit to completion) is exact.
+// No device-side wait exists anywhere: progress is driven by the host calls
+// (submit / poll / wait), and waits are bounded by the caller's timeout.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <chrono>
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "../../include/bsfit.h"
+#include "bsfit_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+int cuda_status_s(cudaError_t e) {
+  if (e == cudaSuccess) return BSFIT_OK;
+  if (e == cudaErrorMemoryAllocation) return BSFIT_E_NOT_ENOUGH_MEMORY;
+  return BSFIT_E_CUDA;
+}
+
+// First-fit allocator over [0, size) with coalescing free list, 256-byte units.
+class Arena {
+ public:
+  void init(int64_t size) {
+    size_ = size;
+    free_.clear();
+    free_[0] = size;
+  }
+  int64_t alloc(int64_t bytes) {
+    bytes = (bytes + 255) / 256 * 256;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        int64_t off = it->first, len = it->second;
+        free_.erase(it);
+        if (len > bytes) free_[off + bytes] = len - bytes;
+        used_ += bytes;
+        return off;
+      }
+    }
+    return -1;
+  }
+  void release(int64_t off, int64_t bytes) {
+    bytes = (bytes + 255) / 256 * 256;
+    used_ -= bytes;
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  int64_t size() const { return size_; }
+  int64_t used() const { return used_; }
+
+ private:
+  int64_t size_ = 0, used_ = 0;
+  std::map<int64_t, int64_t> free_;
+};
+
+struct Request {
+  int64_t id = 0;
+  std::vector<bsfit_host_segment> segs;
+  int64_t bytes = 0;       // arena bytes
+  int64_t offset = -1;     // arena offset
+  int slot = -1;
+  int64_t rois = 0;
+  Clock::time_point submitted, started;
+  std::atomic<int64_t> done_ns{0};  // completion time (ns since epoch of Clock), 0 while running
+  std::atomic<int> finished{0};
+  int status = BSFIT_OK;
+};
+
+void CUDART_CB on_done(void* p) {
+  Request* r = static_cast<Request*>(p);
+  r->done_ns.store(Clock::now().time_since_epoch().count(), std::memory_order_relaxed);
+  r->finished.store(1, std::memory_order_release);
+}
+
+int64_t request_bytes(const std::vector<bsfit_host_segment>& segs) {
+  int64_t b = 256 + (int64_t)segs.size() * 2 * 8;  // work-queue counters
+  for (const auto& g : segs) {
+    const int nv = bsfit_num_params(bsfit_model_fittype(g.model));
+    b += (g.nfits * g.roi_size * g.roi_size * 4 + 255) / 256 * 256;
+    b += ((int64_t)g.nfits * (2 * nv + 2) * 4 + 255) / 256 * 256;
+  }
+  return b;
+}
+
+}  // namespace
+
+struct bsfit_server_s {
+  std::mutex mu;
+  char* arena_base = nullptr;
+  Arena arena;
+  std::vector<cudaStream_t> streams;
+  std::vector<Request*> slot_req;  // request running in each slot, or null
+  std::deque<Request*> pending;
+  std::map<int64_t, Request*> all;  // every request not yet collected
+  std::vector<double> latencies_ms;
+  int64_t next_id = 1;
+  int64_t rois_done = 0;
+  Clock::time_point first_submit;
+  Clock::time_point last_done;
+  bool any_submit = false;
+  int device = 0;
+};
+
+namespace {
+
+// Enqueue an admitted request on its slot's stream. Caller holds the mutex.
+int launch_request(bsfit_server_s* s, Request* r) {
+  cudaStream_t st = s->streams[r->slot];
+  char* base = s->arena_base + r->offset;
+  int64_t off = 0;
+  unsigned long long* scratch = (unsigned long long*)base;
+  off += 256 + (int64_t)r->segs.size() * 2 * 8;
+  off = (off + 255) / 256 * 256;
+  std::vector<bsfit_segment> dsegs(r->segs.size());
+  cudaError_t e = cudaSuccess;
+  for (size_t i = 0; i < r->segs.size(); ++i) {
+    const bsfit_host_segment& g = r->segs[i];
+    const int nv = bsfit_num_params(bsfit_model_fittype(g.model));
+    const int64_t rb = g.nfits * g.roi_size * g.roi_size * 4;
+    float* d_rois = (float*)(base + off);
+    off += (rb + 255) / 256 * 256;
+    float* d_out = (float*)(base + off);
+    off += ((int64_t)g.nfits * (2 * nv + 2) * 4 + 255) / 256 * 256;
+    if (e == cudaSuccess && rb > 0) e = cudaMemcpyAsync(d_rois, g.rois, rb, cudaMemcpyHostToDevice, st);
+    bsfit_segment& d = dsegs[i];
+    d.model = g.model;
+    d.d_rois = d_rois;
+    d.roi_size = g.roi_size;
+    d.nfits = g.nfits;
+    d.iterations = g.iterations;
+    d.d_P = d_out;
+    d.d_CRLB = d_out + g.nfits * (nv + 1);
+    d.d_LL = d.d_CRLB + g.nfits * nv;
+  }
+  if (e != cudaSuccess) return cuda_status_s(e);
+  int stt = bsfit_batch_fit_device(dsegs.data(), (int32_t)dsegs.size(), scratch,
+                                   bsfit_batch_scratch_bytes((int32_t)dsegs.size()), st);
+  if (stt != BSFIT_OK) return stt;
+  for (size_t i = 0; i < r->segs.size(); ++i) {
+    const bsfit_host_segment& g = r->segs[i];
+    const int nv = bsfit_num_params(bsfit_model_fittype(g.model));
+    if (g.nfits == 0) continue;
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(g.P, dsegs[i].d_P, (size_t)g.nfits * (nv + 1) * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(g.CRLB, dsegs[i].d_CRLB, (size_t)g.nfits * nv * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(g.LL, dsegs[i].d_LL, (size_t)g.nfits * 4, cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaLaunchHostFunc(st, on_done, r);
+  return cuda_status_s(e);
+}
+
+// Admit pending requests while slots and arena space allow (submission order).
+void admit(bsfit_server_s* s) {
+  while (!s->pending.empty()) {
+    int slot = -1;
+    for (size_t i = 0; i < s->slot_req.size(); ++i)
+      if (!s->slot_req[i]) {
+        slot = (int)i;
+        break;
+      }
+    if (slot < 0) return;
+    Request* r = s->pending.front();
+    int64_t off = s->arena.alloc(r->bytes);
+    if (off < 0) return;  // wait for memory to free up
+    s->pending.pop_front();
+    r->offset = off;
+    r->slot = slot;
+    r->started = Clock::now();
+    s->slot_req[slot] = r;
+    int st = launch_request(s, r);
+    if (st != BSFIT_OK) {
+      // The request failed to launch: complete it with the error.
+      r->status = st;
+      cudaStreamSynchronize(s->streams[slot]);
+      r->done_ns.store(Clock::now().time_since_epoch().count());
+      r->finished.store(1);
+    }
+  }
+}
+
+// Retire finished requests: free their slot and arena space.
+void retire(bsfit_server_s* s) {
+  for (size_t i = 0; i < s->slot_req.size(); ++i) {
+    Request* r = s->slot_req[i];
+    if (r && r->finished.load(std::memory_order_acquire)) {
+      s->arena.release(r->offset, r->bytes);
+      s->slot_req[i] = nullptr;
+      const Clock::time_point done{Clock::duration(r->done_ns.load())};
+      s->latencies_ms.push_back(std::chrono::duration<double, std::milli>(done - r->submitted).count());
+      s->rois_done += r->rois;
+      if (done > s->last_done) s->last_done = done;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int bsfit_server_create(int32_t max_inflight, int64_t arena_bytes, bsfit_server* out) {
+  if (!out || max_inflight < 1 || max_inflight > 64 || arena_bytes < (1 << 20)) return BSFIT_E_INVALID;
+  *out = nullptr;
+  bsfit_server_s* s = new (std::nothrow) bsfit_server_s;
+  if (!s) return BSFIT_E_NOT_ENOUGH_MEMORY;
+  cudaGetDevice(&s->device);
+  cudaError_t e = cudaMalloc(&s->arena_base, (size_t)arena_bytes);
+  if (e != cudaSuccess) {
+    delete s;
+    return cuda_status_s(e);
+  }
+  s->arena.init(arena_bytes);
+  s->streams.resize(max_inflight, nullptr);
+  s->slot_req.assign(max_inflight, nullptr);
+  for (int i = 0; i < max_inflight && e == cudaSuccess; ++i)
+    e = cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    for (auto st : s->streams)
+      if (st) cudaStreamDestroy(st);
+    cudaFree(s->arena_base);
+    delete s;
+    return cuda_status_s(e);
+  }
+  *out = s;
+  return BSFIT_OK;
+}
+
+int bsfit_server_destroy(bsfit_server s) {
+  if (!s) return BSFIT_E_INVALID;
+  for (auto st : s->streams) cudaStreamSynchronize(st);
+  for (auto st : s->streams) cudaStreamDestroy(st);
+  cudaFree(s->arena_base);
+  for (auto& kv : s->all) delete kv.second;
+  delete s;
+  return BSFIT_OK;
+}
+
+int bsfit_server_submit(bsfit_server s, const bsfit_host_segment* segs, int32_t nseg,
+                        int64_t* request_id) {
+  if (!s || !segs || nseg < 1 || nseg > BSFIT_MAX_SEGMENTS || !request_id) return BSFIT_E_INVALID;
+  for (int i = 0; i < nseg; ++i) {
+    const bsfit_host_segment& g = segs[i];
+    if (!g.model || g.nfits < 0 || (g.nfits > 0 && (!g.rois || !g.P || !g.CRLB || !g.LL)))
+      return BSFIT_E_INVALID;
+    if (g.roi_size < 1 || g.roi_size > 51) return BSFIT_E_SUBREGION_SIZE;
+  }
+  std::lock_guard<std::mutex> lock(s->mu);
+  Request* r = new (std::nothrow) Request;
+  if (!r) return BSFIT_E_NOT_ENOUGH_MEMORY;
+  r->segs.assign(segs, segs + nseg);
+  r->bytes = request_bytes(r->segs);
+  if (r->bytes > s->arena.size()) {
+    delete r;
+    return BSFIT_E_NOT_ENOUGH_MEMORY;  // can never fit the HBM budget
+  }
+  for (const auto& g : r->segs) r->rois += g.nfits;
+  r->id = s->next_id++;
+  r->submitted = Clock::now();
+  if (!s->any_submit) {
+    s->first_submit = r->submitted;
+    s->last_done = r->submitted;
+    s->any_submit = true;
+  }
+  s->all[r->id] = r;
+  s->pending.push_back(r);
+  retire(s);
+  admit(s);
+  *request_id = r->id;
+  return BSFIT_OK;
+}
+
+int bsfit_server_poll(bsfit_server s, int64_t* done_ids, int32_t max_ids, int32_t* n_done) {
+  if (!s || !n_done || (max_ids > 0 && !done_ids)) return BSFIT_E_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  retire(s);
+  admit(s);
+  int n = 0;
+  for (auto it = s->all.begin(); it != s->all.end() && n < max_ids;) {
+    Request* r = it->second;
+    bool running = false;
+    for (auto q : s->slot_req) running |= (q == r);
+    if (r->finished.load(std::memory_order_acquire) && !running) {
+      done_ids[n++] = r->id;
+      delete r;
+      it = s->all.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  *n_done = n;
+  return BSFIT_OK;
+}
+
+int bsfit_server_wait(bsfit_server s, int64_t request_id, double timeout_s) {
+  if (!s) return BSFIT_E_INVALID;
+  const Clock::time_point limit = Clock::now() + std::chrono::duration_cast<Clock::duration>(
+                                                      std::chrono::duration<double>(timeout_s));
+  for (;;) {
+    {
+      std::lock_guard<std::mutex> lock(s->mu);
+      retire(s);
+      admit(s);
+      auto it = s->all.find(request_id);
+      if (it == s->all.end()) return BSFIT_E_INVALID;  // unknown or already collected
+      Request* r = it->second;
+      bool running = false;
+      for (auto q : s->slot_req) running |= (q == r);
+      if (r->finished.load(std::memory_order_acquire) && !running) {
+        int st = r->status;
+        delete r;
+        s->all.erase(it);
+        return st;
+      }
+    }
+    if (Clock::now() > limit) return BSFIT_E_TIMEOUT;
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+int bsfit_server_stats(bsfit_server s, double* p50_ms, double* p99_ms, double* fits_per_s,
+                       int64_t* completed, int64_t* in_flight, int64_t* queued) {
+  if (!s) return BSFIT_E_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  retire(s);
+  std::vector<double> v = s->latencies_ms;
+  std::sort(v.begin(), v.end());
+  auto q = [&](double f) {
+    if (v.empty()) return 0.0;
+    size_t i = (size_t)std::min<double>((double)v.size() - 1, std::ceil(f * (double)v.size()) - 1);
+    return v[i];
+  };
+  if (p50_ms) *p50_ms = q(0.50);
+  if (p99_ms) *p99_ms = q(0.99);
+  if (fits_per_s) {
+    double span = std::chrono::duration<double>(s->last_done - s->first_submit).count();
+    *fits_per_s = span > 0 ? (double)s->rois_done / span : 0.0;
+  }
+  if (completed) *completed = (int64_t)s->latencies_ms.size();
+  int64_t fl = 0;
+  for (auto r : s->slot_req) fl += (r != nullptr);
+  if (in_flight) *in_flight = fl;
+  if (queued) *queued = (int64_t)s->pending.size();
+  return BSFIT_OK;
+}
+
+int bsfit_server_reset_stats(bsfit_server s) {
+  if (!s) return BSFIT_E_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->latencies_ms.clear();
+  s->rois_done = 0;
+  s->any_submit = false;
+  return BSFIT_OK;
+}
+
+}  // extern "C"

@@ -116,6 +116,9 @@ int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
                        bsfit_model* out);
 int bsfit_model_release(bsfit_model model);
 
+/* Fit type of a model (6, 7, 8), 0 for NULL. */
+int32_t bsfit_model_fittype(bsfit_model model);
+
 /*
  * Asynchronous fit on a CUDA stream with device pointers (replaces the launch
  * wrappers VC/GPUmleFit_LM/wrapper.cu:256-279 and their kernels
@@ -182,6 +185,50 @@ int64_t bsfit_batch_scratch_bytes(int32_t nseg);
  * number of claimed and of finished ROIs. Allocates nothing. */
 int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scratch,
                            int64_t scratch_bytes, void* stream);
+
+/*
+ * Serving form (no counterpart in the reference, whose GUI fits one block at a
+ * time, MultiD_fitter/simplefitter_cspline.m:309-313): a continuous-batching
+ * request loop. Each request is a list of segments with HOST buffers (use
+ * page-locked memory for asynchronous copies); requests that arrive while
+ * others run are admitted as slots (max_inflight CUDA streams) and arena memory
+ * (arena_bytes of device memory, reserved once at creation: the HBM budget)
+ * free up, in submission order, and run concurrently on the GPU. A request
+ * completes independently of the others: poll returns the ids of finished
+ * requests (their outputs are filled), wait blocks up to a timeout. Progress
+ * is driven by these calls; no device-side wait exists. Latency = submission to
+ * completion (a host callback at the end of the request's stream).
+ */
+typedef struct bsfit_host_segment {
+  bsfit_model model;
+  const float* rois;     /* host, nfits * roi_size^2 floats */
+  int64_t roi_size;
+  int64_t nfits;
+  int32_t iterations;
+  float* P;              /* host outputs, layout as bsfit_GPUmleFit_LM_multiD */
+  float* CRLB;
+  float* LL;
+} bsfit_host_segment;
+
+typedef struct bsfit_server_s* bsfit_server;
+
+int bsfit_server_create(int32_t max_inflight, int64_t arena_bytes, bsfit_server* out);
+int bsfit_server_destroy(bsfit_server server);
+/* Non-blocking: admits the request or queues it; BSFIT_E_NOT_ENOUGH_MEMORY if it
+ * can never fit the arena. */
+int bsfit_server_submit(bsfit_server server, const bsfit_host_segment* segs, int32_t nseg,
+                        int64_t* request_id);
+/* Retires finished requests, admits queued ones, returns up to max_ids ids of
+ * finished requests (each id is returned once). */
+int bsfit_server_poll(bsfit_server server, int64_t* done_ids, int32_t max_ids, int32_t* n_done);
+/* Blocks until the request finished (its status) or timeout_s passed
+ * (BSFIT_E_TIMEOUT). */
+int bsfit_server_wait(bsfit_server server, int64_t request_id, double timeout_s);
+/* Latency quantiles over completed requests, fits/s from the first submission
+ * to the last completion, and the request counts. Any pointer may be NULL. */
+int bsfit_server_stats(bsfit_server server, double* p50_ms, double* p99_ms, double* fits_per_s,
+                       int64_t* completed, int64_t* in_flight, int64_t* queued);
+int bsfit_server_reset_stats(bsfit_server server);
 
 /*
  * Allocation-free batched fit (no counterpart in the reference). For callers

@@ -1,0 +1,94 @@
+"""Serving form (bsfit_server_*): requests of mixed models and sizes submitted
+while others run give the same results as each request fitted alone through
+the plain call; admission respects the device-memory budget; waits are
+bounded."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bsfit_mod():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import __graft_entry__
+    __graft_entry__.build()
+    import bsfit
+    return bsfit
+
+
+def _frames():
+    from bsfit import workloads as W
+    frames = []
+    for k, (s, n) in enumerate([(13, 3000), (17, 1500), (11, 2500), (13, 800)]):
+        w = W.workload_3d(n, s=s, stream=800 + k)
+        frames.append(("3d", w))
+    frames.append(("4d", W.workload_4d(500, sizes=(15,), stream=810)[0]))
+    frames.append(("5d", W.workload_5d(60, stream=811)))
+    return frames
+
+
+def test_serving_matches_plain_in_the_mix(bsfit_mod):
+    frames = _frames()
+    models = {}
+    for kind, w in frames:
+        if kind not in models:
+            models[kind] = bsfit_mod.Model(w.fittype, w.coeff, coeff3=w.coeff3, init_p=w.init_p)
+    # Arena of 24 MB: the 5D model's frames and the large 3D frames cannot all be
+    # resident at once, so later requests wait for memory and slots.
+    srv = bsfit_mod.Server(max_inflight=3, arena_bytes=24 << 20)
+    ids = [srv.submit([(models[kind], w.rois, w.iterations)]) for kind, w in frames]
+    results = {}
+    for rid in ids:
+        results[rid] = srv.wait(rid, timeout=120.0)
+    st = srv.stats()
+    assert st["completed"] == len(frames) and st["in_flight"] == 0 and st["queued"] == 0
+    assert st["p99_ms"] >= st["p50_ms"] > 0 and st["fits_per_s"] > 0
+    for rid, (kind, w) in zip(ids, frames):
+        kw = {}
+        if w.init_p is not None:
+            kw["initP"] = w.init_p
+        if w.coeff3 is not None:
+            kw["coeff3"] = w.coeff3
+        P, C, L = bsfit_mod.GPUmleFit_LM_multiD(w.rois, w.fittype, w.iterations, w.coeff, **kw)
+        Ps, Cs, Ls = results[rid][0]
+        assert np.array_equal(Ps, P, equal_nan=True), kind
+        assert np.array_equal(Cs, C, equal_nan=True), kind
+        assert np.array_equal(Ls, L, equal_nan=True), kind
+    srv.close()
+
+
+def test_serving_poll_returns_each_request_once(bsfit_mod):
+    from bsfit import workloads as W
+    w = W.workload_3d(1000, s=13, stream=820)
+    m = bsfit_mod.Model(6, w.coeff)
+    srv = bsfit_mod.Server(max_inflight=2, arena_bytes=64 << 20)
+    ids = {srv.submit([(m, w.rois[i * 100:(i + 1) * 100], 30)]) for i in range(10)}
+    seen = {}
+    import time
+    t0 = time.time()
+    while len(seen) < len(ids) and time.time() - t0 < 60:
+        for rid, res in srv.poll().items():
+            assert rid not in seen
+            seen[rid] = res
+    assert set(seen) == ids
+    srv.close()
+
+
+def test_serving_budget_and_timeout(bsfit_mod):
+    from bsfit import _native, workloads as W
+    w = W.workload_3d(20000, s=17, stream=821)
+    m = bsfit_mod.Model(6, w.coeff)
+    srv = bsfit_mod.Server(max_inflight=1, arena_bytes=8 << 20)
+    with pytest.raises(bsfit_mod.BsfitError) as e:
+        srv.submit([(m, w.rois, 30)])  # 23 MB of ROIs > 8 MB budget
+    assert e.value.status == 6
+    srv.close()
+    srv = bsfit_mod.Server(max_inflight=1, arena_bytes=64 << 20)
+    rid = srv.submit([(m, w.rois, 30)])
+    st = _native.lib().bsfit_server_wait(srv._h, rid, 0.0)
+    assert st in (0, 12)  # done already, or BSFIT_E_TIMEOUT
+    srv.wait(rid, timeout=120.0)
+    srv.close()

@@ -172,6 +172,83 @@ def bench_reference(args):
     return 0
 
 
+def bench_serving(args, dev, seed=11):
+    """Mixed-model acquisition stream through the serving form, against the
+    plain per-call form (one synchronous GPUmleFit_LM_multiD call per frame).
+
+    Frames: 3D 13 px (60%), 4D 13 px (25%), 5D 17 px (15%) models, frame sizes
+    log-uniform in 2k-50k ROIs (2k-8k for 5D). The stream is run saturated (all
+    frames submitted at once) for throughput, then replayed with Poisson
+    arrivals at ~70% of the saturated rate for latency. A second stream of 10k
+    ROI 3D frames at the same load gives the per-frame latency."""
+    import bsfit
+    from bsfit import workloads as W
+    rng = np.random.default_rng(seed)
+    pools = {"3d": W.workload_3d(200000, s=13, stream=21),
+             "4d": W.workload_4d(60000, sizes=(13,), stream=22)[0],
+             "5d": W.workload_5d(12000, s=17, stream=23)}
+    models = {k: bsfit.Model(w.fittype, w.coeff, coeff3=w.coeff3, init_p=w.init_p) for k, w in pools.items()}
+    frames = []
+    for _ in range(args.serve_frames):
+        kind = rng.choice(["3d", "4d", "5d"], p=[0.6, 0.25, 0.15])
+        hi = 8000 if kind == "5d" else 50000
+        n = int(np.exp(rng.uniform(np.log(2000), np.log(hi))))
+        w = pools[kind]
+        o = int(rng.integers(0, len(w.rois) - n))
+        frames.append((kind, w, np.ascontiguousarray(w.rois[o:o + n])))
+    n_rois = sum(len(f[2]) for f in frames)
+
+    def run_stream(srv, frame_list, gaps):
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        ids = []
+        for (kind, w, r), gap in zip(frame_list, gaps):
+            if gap > 0:
+                target = time.perf_counter() + gap
+                while time.perf_counter() < target:
+                    srv.poll()
+            ids.append(srv.submit([(models[kind], r, w.iterations)]))
+        for rid in ids:
+            srv.wait(rid, timeout=300.0)
+        el = time.perf_counter() - t0
+        return el, srv.stats()
+
+    srv = bsfit.Server(max_inflight=4, arena_bytes=4 << 30)
+    run_stream(srv, frames[:4], [0] * 4)  # warm-up
+    sat_s, sat = run_stream(srv, frames, [0] * len(frames))
+    rate = 0.7 * len(frames) / sat_s
+    gaps = rng.exponential(1.0 / rate, len(frames))
+    gaps[0] = 0
+    load_s, loaded = run_stream(srv, frames, gaps)
+    # 10k-ROI 3D frames at the same load
+    w3 = pools["3d"]
+    f10 = [("3d", w3, np.ascontiguousarray(w3.rois[i * 10000:(i + 1) * 10000])) for i in range(20)]
+    s10_s, s10 = run_stream(srv, f10, [0] * len(f10))
+    g10 = rng.exponential(len(f10) / (0.7 * len(f10) / s10_s) / len(f10), len(f10))
+    g10[0] = 0
+    _, l10 = run_stream(srv, f10, g10)
+    srv.close()
+    # plain per-call form
+    t0 = time.perf_counter()
+    for kind, w, r in frames:
+        kw = {}
+        if w.init_p is not None:
+            kw["initP"] = w.init_p
+        if w.coeff3 is not None:
+            kw["coeff3"] = w.coeff3
+        bsfit.GPUmleFit_LM_multiD(r, w.fittype, w.iterations, w.coeff, **kw)
+    plain_s = time.perf_counter() - t0
+    return {"stream": f"{len(frames)} frames, {n_rois} ROIs: 3D 13px 60%, 4D 13px 25%, 5D 17px 15%, "
+                      f"2k-50k ROIs per frame (2k-8k for 5D)",
+            "fits_per_s": n_rois / sat_s, "plain_fits_per_s": n_rois / plain_s,
+            "speedup_vs_plain": plain_s / sat_s,
+            "load": 0.7, "p50_ms": loaded["p50_ms"], "p99_ms": loaded["p99_ms"],
+            "loaded_fits_per_s": n_rois / load_s,
+            "frame10k_3d": {"p50_ms": l10["p50_ms"], "p99_ms": l10["p99_ms"], "load": 0.7,
+                            "saturated_p50_ms": s10["p50_ms"]},
+            "max_inflight": 4, "arena_bytes": 4 << 30}
+
+
 def bench_gpu(args):
     import torch
     import bsfit
@@ -284,6 +361,7 @@ def bench_gpu(args):
             b5.record(stream)
         stream.synchronize()
         fits_5d17 = len(w5.rois) / (a5.elapsed_time(b5) / 2 * 1e-3)
+    serving = None if args.no_serve else bench_serving(args, dev)
     if rank != 0:
         return 0
     cpu_n, cpu_t = run_cpu(groups, os.cpu_count() or 1, 0.016)
@@ -325,6 +403,7 @@ def bench_gpu(args):
                                    f"the reference CPU fitter, OpenMP over ROIs"},
         "fits_per_s": {"3d_13px": fits_3d13, "5d_17px": fits_5d17,
                        "5d_workload": f"{args.rois_5d} ROIs 17x17, fit type 8, 60 iterations"},
+        "serving": serving,
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
     }
@@ -344,6 +423,8 @@ def main():
     ap.add_argument("--sizes", type=int, nargs="+", default=list(SIZES))
     ap.add_argument("--rois-5d", type=int, default=50000, help="ROIs of the 5D 17 px figure")
     ap.add_argument("--no-5d", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-frames", type=int, default=80)
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)

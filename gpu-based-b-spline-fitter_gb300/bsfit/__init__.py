@@ -204,6 +204,7 @@ class Server:
                                                 np.ctypeslib.ctypes.byref(h)), "bsfit_server_create")
         self._h = h
         self._live = {}
+        self._done = {}  # results collected by poll() and not yet taken by wait()
 
     def submit(self, entries):
         import torch
@@ -245,10 +246,13 @@ class Server:
             check(_native.lib().bsfit_server_poll(self._h, ids, 256, ct.byref(n)), "bsfit_server_poll")
             for i in range(n.value):
                 out[ids[i]] = self._results(ids[i])
+                self._done[ids[i]] = out[ids[i]]
             if n.value < 256:
                 return out
 
     def wait(self, rid, timeout=60.0):
+        if rid in self._done:
+            return self._done.pop(rid)
         check(_native.lib().bsfit_server_wait(self._h, int(rid), float(timeout)), "bsfit_server_wait")
         return self._results(rid)
 

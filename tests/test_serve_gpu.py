@@ -73,6 +73,7 @@ def test_serving_poll_returns_each_request_once(bsfit_mod):
         for rid, res in srv.poll().items():
             assert rid not in seen
             seen[rid] = res
+            srv.wait(rid)  # taken from the poll()ed results
     assert set(seen) == ids
     srv.close()
 

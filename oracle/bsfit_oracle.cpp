@@ -186,8 +186,10 @@ void derivative(const T* pos, const int* n, const T* wf, T* const* wd, const T* 
     int lv[5];
     for (int a = 0; a < D; ++a) lv[a] = ((nIndex >> a) & 1) + 1;
     long long node[32];
+#pragma GCC unroll 32
     for (int b = 0; b < B; ++b) {
       long long idx = 0;
+#pragma GCC unroll 5
       for (int a = 0; a < D; ++a) {
         bool side2 = (b >> a) & 1;
         int kk = side2 ? (k[a] + lv[a] - 1) : (k[a] - lv[a]);
@@ -196,10 +198,13 @@ void derivative(const T* pos, const int* n, const T* wf, T* const* wd, const T* 
       node[b] = idx;
     }
     T s = cmat[node[0]] * wf[B * nIndex];
+#pragma GCC unroll 32
     for (int b = 1; b < B; ++b) s = s + cmat[node[b]] * wf[B * nIndex + b];
     f += s;
+#pragma GCC unroll 5
     for (int d = 0; d < D; ++d) {
       double sd = 0.0;
+#pragma GCC unroll 32
       for (int b = 0; b < B; ++b) {
         long long nd = node[b];
         T w = wd[d][B * nIndex + b];

@@ -1,4 +1,4 @@
-"""bsfit: GB300-native B-spline PSF MLE fitter (fit types 6, 7, 8).
+"""bsfit: GB300-native B-spline PSF MLE fitter (fit types 6, 7, 8 and the 4Pi fit).
 
 Python mirror of the reference's MATLAB call surface over the C ABI of
 libbsfit.so:
@@ -17,6 +17,7 @@ from . import _native
 from ._native import BsfitError, check
 
 NUM_PARAMS = {6: 5, 7: 6, 8: 8}
+FIT_4PI = 9  # model tag of 4Pi models (BSFIT_FITTYPE_4PI)
 
 _fp = _native._fp
 
@@ -130,6 +131,104 @@ class Model:
         check(_native.lib().bsfit_eval_device(self._h, rois.data_ptr(), s, n, theta.data_ptr(),
                                               int(bool(fisher)), out.data_ptr(), st.cuda_stream),
               "bsfit_eval_device")
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.lib().bsfit_model_release(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def GPUmleFit_LM_4Pi_bspline(imstack, shared, iterations, coeff, dT, initZ, initPhi,
+                             phase_shift, silent=1):
+    """Drop-in for the reference's 4Pi mex (demo_4pi/bspline_based_4piloc_v4.m:196).
+
+    imstack: (4, N, s, s) float32 (the C-order view of MATLAB [s, s, N, 4]);
+    shared: 6 flags (all 1); coeff: (W, Z, X, Y) 4D coefficients; dT: (N, 4, 6)
+    (MATLAB [6, 4, N]); initZ, initPhi: (N,); phase_shift: (4,). Returns P
+    (N, 7), CRLB (N, 6), LL (N,)."""
+    lib = _native.lib()
+    im = _f32(imstack)
+    if im.ndim == 3:
+        im = im[:, None]
+    if im.ndim != 4:
+        raise ValueError("imstack must be (4, N, s, s)")
+    ch, n, s2, s1 = im.shape
+    sh = np.ascontiguousarray(np.atleast_1d(shared), dtype=np.uint32)
+    c = _f32(coeff)
+    dt = _f32(dT)
+    z0 = _f32(np.atleast_1d(initZ))
+    w0 = _f32(np.atleast_1d(initPhi))
+    ps = _f32(np.atleast_1d(phase_shift))
+    P = np.zeros((7, n), np.float32)
+    C = np.zeros((6, n), np.float32)
+    L = np.zeros(n, np.float32)
+    ptr = lambda a: a.ctypes.data_as(_fp)  # noqa: E731
+    st = lib.bsfit_GPUmleFit_LM_4Pi_bspline(
+        ptr(im), s1, s2, n, ch, sh.ctypes.data_as(np.ctypeslib.ctypes.POINTER(
+            np.ctypeslib.ctypes.c_uint32)), sh.size, int(iterations), ptr(c), c.ndim, _dims(c),
+        ptr(dt), dt.size, ptr(z0), z0.size, ptr(w0), w0.size, ptr(ps), ps.size, int(silent),
+        ptr(P), ptr(C), ptr(L))
+    check(st, "GPUmleFit_LM_4Pi_bspline")
+    return P.T.copy(), C.T.copy(), L
+
+
+class Model4Pi:
+    """A 4Pi model (4D phase-resolved coefficients and the four channels'
+    phase shifts in knot units) resident on the device."""
+
+    nv = 6
+    channels = 4
+
+    def __init__(self, coeff, phase_shift):
+        lib = _native.lib()
+        c = _f32(coeff)
+        ps = _f32(np.atleast_1d(phase_shift))
+        if ps.size != self.channels:
+            raise ValueError("phase_shift must hold 4 values")
+        h = np.ctypeslib.ctypes.c_void_p()
+        check(lib.bsfit_model_create_4pi(c.ctypes.data_as(_fp), c.ndim, _dims(c),
+                                         ps.ctypes.data_as(_fp), ps.size,
+                                         np.ctypeslib.ctypes.byref(h)), "bsfit_model_create_4pi")
+        self._h = h
+
+    def fit_torch(self, rois, iterations, initZ, initPhi, dT=None, stream=None):
+        """rois: CUDA float32 (4, N, s, s); initZ, initPhi: (N,); dT: (N, 4, 6)
+        or None. Returns (P (7, N), CRLB (6, N), LL (N,)) device tensors."""
+        import torch
+        assert rois.is_cuda and rois.dtype == torch.float32 and rois.is_contiguous()
+        n, s = rois.shape[1], rois.shape[-1]
+        z0 = initZ.contiguous()
+        w0 = initPhi.contiguous()
+        dt = dT.contiguous() if dT is not None else None
+        P = torch.empty((7, n), device=rois.device, dtype=torch.float32)
+        C = torch.empty((6, n), device=rois.device, dtype=torch.float32)
+        L = torch.empty((n,), device=rois.device, dtype=torch.float32)
+        st = stream if stream is not None else torch.cuda.current_stream(rois.device)
+        check(_native.lib().bsfit_fit4pi_device(
+            self._h, rois.data_ptr(), s, n, int(iterations),
+            dt.data_ptr() if dt is not None else None, z0.data_ptr(), w0.data_ptr(),
+            P.data_ptr(), C.data_ptr(), L.data_ptr(), st.cuda_stream), "bsfit_fit4pi_device")
+        return P, C, L
+
+    def eval_torch(self, rois, theta, dT=None, fisher=False, stream=None):
+        """One 4Pi evaluation per ROI at theta (6, N); returns (N, 1 + 6 + 21)."""
+        import torch
+        n, s = rois.shape[1], rois.shape[-1]
+        out = torch.empty((n, 28), device=rois.device, dtype=torch.float32)
+        theta = theta.contiguous()
+        dt = dT.contiguous() if dT is not None else None
+        st = stream if stream is not None else torch.cuda.current_stream(rois.device)
+        check(_native.lib().bsfit_eval4pi_device(
+            self._h, rois.data_ptr(), s, n, dt.data_ptr() if dt is not None else None,
+            theta.data_ptr(), int(bool(fisher)), out.data_ptr(), st.cuda_stream),
+            "bsfit_eval4pi_device")
         return out
 
     def close(self):
@@ -291,7 +390,10 @@ def eval_flops(fittype, s, channels=1):
     """Algorithmic FLOPs of one ROI evaluation (separable minimum): contract the
     non-lateral axes over the (s+4)^2 knot window, one 4-tap pass per lateral
     axis and output map, then the Jacobian, Hessian and deviance per pixel.
-    K = 4^(D-2) coefficients per lateral node."""
+    K = 4^(D-2) coefficients per lateral node. The 4Pi fit (FIT_4PI) is the
+    4D evaluation once per channel."""
+    if fittype == FIT_4PI:
+        return 4 * eval_flops(7, s, channels)
     d = {6: 3, 7: 4, 8: 5}[fittype]
     nv = NUM_PARAMS[fittype]
     k = 4 ** (d - 2)

@@ -52,6 +52,20 @@ SIGNATURES = {
     "bsfit_fit_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "bsfit_GPUmleFit_LM_4Pi_bspline": (ctypes.c_int, [
+        _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+        ctypes.POINTER(ctypes.c_uint32), ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int32,
+        _i64p, _fp, ctypes.c_int64, _fp, ctypes.c_int64, _fp, ctypes.c_int64, _fp,
+        ctypes.c_int64, ctypes.c_int32, _fp, _fp, _fp]),
+    "bsfit_model_create_4pi": (ctypes.c_int, [
+        _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "bsfit_fit4pi_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p]),
+    "bsfit_eval4pi_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 

@@ -55,7 +55,8 @@ class Workload:
 
     @property
     def n_fits(self):
-        return self.rois.shape[0]
+        # 4Pi ROIs are (channels, N, s, s)
+        return self.rois.shape[1] if self.rois.ndim == 4 else self.rois.shape[0]
 
 
 def _rng(stream):
@@ -321,3 +322,80 @@ def workload_5d(n=100_000, s=17, iterations=60, stream=5):
     init_p = np.array([z_to_param(0.0, -400.0), phi_to_w(np.pi), theta_to_u(np.deg2rad(40.0)),
                        0.7], dtype=np.float32)
     return Workload(f"5d_{s}px", 8, iterations, c5, rois, truth, init_p=init_p, coeff3=c3)
+
+
+# ---------------------------------------------------------------------------
+# 4Pi model (four interference channels, GPUmleFit_LM_4Pi_bspline)
+
+N_PHI = 32                       # phase knots per period
+PHI_STEP = 2 * np.pi / N_PHI
+LAMBDA_NM = 668.0                # emission wavelength of the reference's demo
+PHASE_SHIFTS = np.array([0.0, 0.5 * np.pi, np.pi, 1.5 * np.pi])
+
+
+def modulation(z_nm):
+    """Interference contrast of the synthetic 4Pi PSF (falls off with |z|)."""
+    return 0.8 * np.exp(-(np.asarray(z_nm) / 900.0) ** 2)
+
+
+def psf4pi_samples(n_lat=26, z_lo=-600.0, z_hi=600.0):
+    """Phase-resolved PSF stack (W, Z, X, Y): the astigmatic PSF times
+    1 + m(z) cos(phase), at phases 0 .. (N_PHI + 1) * PHI_STEP (one period plus
+    one sample, as bspline_based_4piloc_v4.m:80-86 samples it)."""
+    base, z = psf3d_samples(n_lat, z_lo, z_hi)
+    ph = PHI_STEP * np.arange(N_PHI + 2)
+    m = modulation(z)
+    out = base[None] * (1.0 + m[None, :, None, None] * np.cos(ph)[:, None, None, None])
+    return out, z
+
+
+def coeff4pi(n_lat=26):
+    """Mirror-prefiltered coefficients (W, Z, X, Y): W = N_PHI + 4 along the phase
+    axis, so the fitter's period is W - 4 = N_PHI knots."""
+    key = ("4pi", n_lat)
+    if key not in _COEFF_CACHE:
+        s, _ = psf4pi_samples(n_lat)
+        _COEFF_CACHE[key] = _coeff_f32(s)
+    return _COEFF_CACHE[key]
+
+
+def phase_to_w(phi):
+    """Phase (rad) to the fit's phase position: knot units with the +1 origin
+    (simBSplinePSF.m: wc = Phi / dphidN + 1)."""
+    return np.mod(np.asarray(phi), 2 * np.pi) / PHI_STEP + 1.0
+
+
+def rois4pi(n, s, rng, z_range=500.0, n_lo=1000.0, n_hi=5000.0, bg_lo=10.0, bg_hi=30.0,
+            xy_spread=1.0):
+    """Poisson ROIs of the four channels, (4, N, s, s); photons and background
+    per channel, shared by the channels; phase = 4 pi z / lambda."""
+    cx = (s - 1) / 2.0
+    x = cx + rng.uniform(-xy_spread, xy_spread, n)
+    y = cx + rng.uniform(-xy_spread, xy_spread, n)
+    z = rng.uniform(-z_range, z_range, n)
+    phi = np.mod(4 * np.pi * z / LAMBDA_NM, 2 * np.pi)
+    photons = np.exp(rng.uniform(math.log(n_lo), math.log(n_hi), n))
+    bg = rng.uniform(bg_lo, bg_hi, n)
+    sx, sy = astig_sigmas(z, 1.3)
+    base = _int_gauss(x, sx, s)[:, :, None] * _int_gauss(y, sy, s)[:, None, :]
+    m = modulation(z)
+    rois = np.empty((4, n, s, s), np.float32)
+    for c, sh in enumerate(PHASE_SHIFTS):
+        mod = 1.0 + m * np.cos(phi + sh)
+        model = bg[:, None, None] + photons[:, None, None] * mod[:, None, None] * base
+        rois[c] = rng.poisson(model)
+    truth = dict(x=x, y=y, z_nm=z, z=z_to_param(z), phi=phi, w=phase_to_w(phi), N=photons, bg=bg)
+    return rois, truth
+
+
+def workload_4pi(n=100_000, s=13, iterations=100, stream=6, start_phase=2 * np.pi):
+    """4Pi fit as the reference's demo runs it: 13 px ROIs in four channels,
+    100 iterations, z started mid-range and the phase at one start value."""
+    rng = _rng(stream)
+    rois, truth = rois4pi(n, s, rng)
+    init_z = np.full(n, z_to_param(0.0), np.float32)
+    init_phi = np.full(n, start_phase / PHI_STEP, np.float32)
+    dT = np.zeros((n, 4, 6), np.float32)
+    extra = dict(dT=dT, init_z=init_z, init_phi=init_phi,
+                 phase_shift=(PHASE_SHIFTS / PHI_STEP).astype(np.float32))
+    return Workload(f"4pi_{s}px", 9, iterations, coeff4pi(), rois, truth, extra=extra)

@@ -106,6 +106,8 @@ const char* bsfit_status_str(int status) {
     case BSFIT_E_TIMEOUT: return "bounded device wait timed out";
     case BSFIT_E_STATIC_LIMIT:
       return "too many segments for the allocation-free entry point (its fixed scratch holds 48)";
+    case BSFIT_E_UNSHARED:
+      return "4Pi fit: only four channels with all six parameters shared are supported";
     default: return "unknown status";
   }
 }
@@ -173,6 +175,7 @@ int bsfit_model_release(bsfit_model model) {
 int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
                      int32_t iterations, float* d_P, float* d_CRLB, float* d_LL, void* stream) {
   if (!model) return BSFIT_E_INVALID;
+  if (model->dev.fittype == bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
   if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
   if (nfits < 0) return BSFIT_E_INVALID;
   if (nfits == 0) return BSFIT_OK;
@@ -199,6 +202,7 @@ int bsfit_trace_device(bsfit_model model, const float* d_rois, int64_t roi_size,
                        int32_t iterations, int32_t flags, float* d_P, float* d_CRLB, float* d_LL,
                        float* d_trace, int32_t trace_max, void* stream) {
   if (!model) return BSFIT_E_INVALID;
+  if (model->dev.fittype == bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
   if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
   if (nfits < 0 || trace_max < 0) return BSFIT_E_INVALID;
   if (nfits == 0) return BSFIT_OK;
@@ -223,6 +227,7 @@ int bsfit_trace_device(bsfit_model model, const float* d_rois, int64_t roi_size,
 int bsfit_eval_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
                       const float* d_theta, int32_t fisher, float* d_out, void* stream) {
   if (!model) return BSFIT_E_INVALID;
+  if (model->dev.fittype == bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
   if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
   if (nfits < 0) return BSFIT_E_INVALID;
   if (nfits == 0) return BSFIT_OK;
@@ -249,6 +254,7 @@ int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scra
   for (int i = 0; i < nseg; ++i) {
     const bsfit_segment& g = segs[i];
     if (!g.model) return BSFIT_E_INVALID;
+    if (g.model->dev.fittype == bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
     if (g.roi_size < 1 || g.roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
     if (g.nfits < 0) return BSFIT_E_INVALID;
     if (g.nfits > 0 && (!g.d_rois || !g.d_P || !g.d_CRLB || !g.d_LL)) return BSFIT_E_INVALID;
@@ -361,6 +367,174 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
   if (e == cudaSuccess) e = cudaMemcpyAsync(CRLB, d_C, (size_t)nfits * nv * sizeof(float), cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(LL, d_L, (size_t)nfits * sizeof(float), cudaMemcpyDeviceToHost, stream);
   if (d_rois) cudaFreeAsync(d_rois, stream);
+  if (d_out) cudaFreeAsync(d_out, stream);
+  cudaError_t e2 = stream ? cudaStreamSynchronize(stream) : cudaSuccess;
+  if (stream) cudaStreamDestroy(stream);
+  bsfit_model_release(model);
+  if (st) return st;
+  if (e == cudaSuccess) e = e2;
+  return cuda_status(e);
+}
+
+// ---------------------------------------------------------------------------
+// 4Pi fit (GPUmleFit_LM_4Pi_bspline, demo_4pi/bspline_based_4piloc_v4.m:196-216).
+
+int bsfit_model_create_4pi(const float* coeff, int32_t coeff_ndim, const int64_t* coeff_dims,
+                           const float* phase_shift, int32_t n_channels, bsfit_model* out) {
+  if (!out) return BSFIT_E_INVALID;
+  *out = nullptr;
+  if (!coeff || !phase_shift) return BSFIT_E_WRONG_DATA_TYPE;
+  if (n_channels != bsfit::k4PiChannels) return BSFIT_E_UNSHARED;
+  int st = check_coeff(7, coeff_ndim, coeff_dims);  // a 4D array, as for fit type 7
+  if (st) return st;
+  for (int c = 0; c < bsfit::k4PiChannels; ++c)
+    if (!(phase_shift[c] == phase_shift[c]) || phase_shift[c] > 1e6f || phase_shift[c] < -1e6f)
+      return BSFIT_E_INVALID;
+  bsfit_model_s* m = new (std::nothrow) bsfit_model_s;
+  if (!m) return BSFIT_E_NOT_ENOUGH_MEMORY;
+  fill_model(m->dev, 7, coeff_dims, nullptr, 0);
+  m->dev.fittype = bsfit::kFit4Pi;
+  for (int c = 0; c < bsfit::k4PiChannels; ++c) m->dev.shift[c] = phase_shift[c];
+  const size_t bytes = (size_t)numel(coeff_ndim, coeff_dims) * sizeof(float);
+  cudaError_t e = cudaMalloc(&m->d_coeff, bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_coeff, coeff, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(m->d_coeff);
+    delete m;
+    return cuda_status(e);
+  }
+  m->dev.coeff = m->d_coeff;
+  *out = m;
+  return BSFIT_OK;
+}
+
+int bsfit_fit4pi_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                        int32_t iterations, const float* d_dT, const float* d_initZ,
+                        const float* d_initPhi, float* d_P, float* d_CRLB, float* d_LL,
+                        void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  if (model->dev.fittype != bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_initZ || !d_initPhi || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  a.out_n = nfits;
+  a.dT = d_dT;
+  a.z0 = d_initZ;
+  a.w0 = d_initPhi;
+  return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
+}
+
+int bsfit_eval4pi_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                         const float* d_dT, const float* d_theta, int32_t fisher, float* d_out,
+                         void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  if (model->dev.fittype != bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_theta || !d_out) return BSFIT_E_INVALID;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.dT = d_dT;
+  return cuda_status(bsfit::launch_eval(a, d_theta, d_out, fisher, (cudaStream_t)stream));
+}
+
+int bsfit_GPUmleFit_LM_4Pi_bspline(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                                   int64_t nfits, int64_t n_channels, const uint32_t* shared,
+                                   int64_t shared_numel, int32_t iterations, const float* coeff,
+                                   int32_t coeff_ndim, const int64_t* coeff_dims, const float* dT,
+                                   int64_t dT_numel, const float* initZ, int64_t initZ_numel,
+                                   const float* initPhi, int64_t initPhi_numel,
+                                   const float* phase_shift, int64_t phase_shift_numel,
+                                   int32_t silent, float* P, float* CRLB, float* LL) {
+  constexpr int NV = 6, C = bsfit::k4PiChannels;
+  if (!imstack || !coeff || !dT || !initZ || !initPhi || !phase_shift || !shared)
+    return BSFIT_E_WRONG_DATA_TYPE;
+  if (roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (roi_size2 != roi_size) return BSFIT_E_SUBREGION_SHAPE;
+  if (roi_size < 1 || nfits < 0) return BSFIT_E_INVALID;
+  if (n_channels != C || phase_shift_numel != C) return BSFIT_E_UNSHARED;
+  if (shared_numel != NV) return BSFIT_E_UNSHARED;
+  for (int i = 0; i < NV; ++i)
+    if (shared[i] != 1u) return BSFIT_E_UNSHARED;
+  if (dT_numel != (int64_t)NV * C * nfits || initZ_numel != nfits || initPhi_numel != nfits)
+    return BSFIT_E_WRONG_NO_ARGS;
+  if (!P || !CRLB || !LL) return BSFIT_E_INVALID;
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count < 1) return BSFIT_E_NO_DEVICE;
+  if (!silent) {
+    std::printf("subregion size: %lld channels: %d\n", (long long)roi_size, C);
+    std::printf("Number of fits: %lld no padding\n", (long long)nfits);
+  }
+  bsfit_model model = nullptr;
+  int st = bsfit_model_create_4pi(coeff, coeff_ndim, coeff_dims, phase_shift, C, &model);
+  if (st) return st;
+  if (nfits == 0) {
+    bsfit_model_release(model);
+    return BSFIT_OK;
+  }
+  const size_t s2 = (size_t)roi_size * roi_size;
+  const size_t in_floats = (size_t)nfits * (s2 * C + NV * C + 2);
+  const size_t out_floats = (size_t)nfits * (2 * NV + 2);
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+      (double)((in_floats + out_floats) * sizeof(float)) > 0.95 * (double)free_b) {
+    bsfit_model_release(model);
+    return BSFIT_E_NOT_ENOUGH_MEMORY;
+  }
+  cudaStream_t stream = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  float *d_in = nullptr, *d_out = nullptr;
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_in, in_floats * sizeof(float), stream);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_out, out_floats * sizeof(float), stream);
+  float* d_rois = d_in;
+  float* d_dT = d_rois + (size_t)nfits * s2 * C;
+  float* d_z = d_dT + (size_t)nfits * NV * C;
+  float* d_w = d_z + nfits;
+  // MATLAB [s, s, N, 4] and [6, 4, N] are exactly the device layouts.
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_rois, imstack, (size_t)nfits * s2 * C * sizeof(float),
+                        cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_dT, dT, (size_t)nfits * NV * C * sizeof(float), cudaMemcpyHostToDevice,
+                        stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_z, initZ, (size_t)nfits * sizeof(float), cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_w, initPhi, (size_t)nfits * sizeof(float), cudaMemcpyHostToDevice,
+                        stream);
+  float* d_P = d_out;
+  float* d_C = d_P + (size_t)nfits * (NV + 1);
+  float* d_L = d_C + (size_t)nfits * NV;
+  if (e == cudaSuccess) {
+    st = bsfit_fit4pi_device(model, d_rois, roi_size, nfits, iterations, d_dT, d_z, d_w, d_P,
+                             d_C, d_L, stream);
+    if (st) e = cudaErrorUnknown;
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P, d_P, (size_t)nfits * (NV + 1) * sizeof(float), cudaMemcpyDeviceToHost,
+                        stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(CRLB, d_C, (size_t)nfits * NV * sizeof(float), cudaMemcpyDeviceToHost,
+                        stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(LL, d_L, (size_t)nfits * sizeof(float), cudaMemcpyDeviceToHost, stream);
+  if (d_in) cudaFreeAsync(d_in, stream);
   if (d_out) cudaFreeAsync(d_out, stream);
   cudaError_t e2 = stream ? cudaStreamSynchronize(stream) : cudaSuccess;
   if (stream) cudaStreamDestroy(stream);

@@ -1,5 +1,7 @@
 // Per-ROI Levenberg-Marquardt Poisson-MLE fit of a cubic B-spline PSF,
-// one warp per ROI, for fit types 6 (3D), 7 (4D colour) and 8 (5D + 3D).
+// one warp per ROI, for fit types 6 (3D), 7 (4D colour) and 8 (5D + 3D), and
+// the four-channel 4Pi fit (model tag kFit4Pi: one 4D (x, y, z, phase) spline
+// seen by four interference channels at shifted phases, shared parameters).
 //
 // Method: the reference CPU fitter, VC/CPUmleFit_LM/CPUmleFit_LM.cpp:2411-3620
 // (VC = "MultiD_bspline/visual code"), with the same initial guesses, damping
@@ -74,10 +76,11 @@ struct ModeTraits;
 
 template <>
 struct ModeTraits<6> {
-  static constexpr int D = 3;   // spline dimensions
-  static constexpr int NV = 5;  // fitted parameters
-  static constexpr int NA = 2;  // non-lateral maps: value, d/dz
-  static constexpr int NG = 3;  // after the Y pass: value, d/dY, d/dz
+  static constexpr int D = 3;    // spline dimensions
+  static constexpr int NV = 5;   // fitted parameters
+  static constexpr int NA = 2;   // non-lateral maps: value, d/dz
+  static constexpr int NG = 3;   // after the Y pass: value, d/dY, d/dz
+  static constexpr int NCH = 1;  // image channels per ROI
 };
 template <>
 struct ModeTraits<7> {
@@ -85,6 +88,16 @@ struct ModeTraits<7> {
   static constexpr int NV = 6;
   static constexpr int NA = 3;  // value, d/dz, d/dw
   static constexpr int NG = 4;  // value, d/dY, d/dz, d/dw
+  static constexpr int NCH = 1;
+};
+// 4Pi: the 4D evaluation of fit type 7 once per channel.
+template <>
+struct ModeTraits<kFit4Pi> {
+  static constexpr int D = 4;
+  static constexpr int NV = 6;  // x, y, N, bg, z, phase
+  static constexpr int NA = 3;
+  static constexpr int NG = 4;
+  static constexpr int NCH = k4PiChannels;
 };
 
 template <>
@@ -98,16 +111,19 @@ struct ModeTraits<8> {
   // value, d/dY, d/dz, d/dw, d/du, z correction, u correction (5D); value,
   // d/dY, d/dz (3D)
   static constexpr int NG = 10;
+  static constexpr int NCH = 1;
 };
 
-// Per-warp shared-memory layout (floats). WP = s + 4 bounds the knot window
-// along each lateral axis.
+// Per-warp shared-memory layout (floats): the ROI's pixels (one plane per
+// channel), the per-pixel knots, the 1-D weights, the 4Pi channel offsets, and
+// the A and G maps. WP = s + 4 bounds the knot window along each lateral axis.
 struct WarpLayout {
-  int s, s2p, wp, na, ng;
-  __host__ __device__ int off_kx() const { return s2p; }
+  int s, s2p, wp, na, ng, nch;
+  __host__ __device__ int off_kx() const { return nch * s2p; }
   __host__ __device__ int off_ky() const { return s2p + ((s + 3) & ~3); }
   __host__ __device__ int off_w() const { return off_ky() + ((s + 3) & ~3); }
-  __host__ __device__ int off_a() const { return off_w() + 40; }
+  __host__ __device__ int off_dt() const { return off_w() + 40; }
+  __host__ __device__ int off_a() const { return off_dt() + (nch > 1 ? nch * 6 : 0); }
   __host__ __device__ int off_g() const { return off_a() + na * wp * wp; }
   __host__ __device__ int total() const { return off_g() + ng * wp * s; }
 };
@@ -117,8 +133,9 @@ __host__ __device__ inline WarpLayout make_layout(int mode, int s) {
   L.s = s;
   L.s2p = (s * s + 3) & ~3;
   L.wp = s + 4;
-  L.na = mode == 6 ? 2 : mode == 7 ? 3 : 8;
-  L.ng = mode == 6 ? 3 : mode == 7 ? 4 : 10;
+  L.na = mode == 6 ? 2 : (mode == 7 || mode == kFit4Pi) ? 3 : 8;
+  L.ng = mode == 6 ? 3 : (mode == 7 || mode == kFit4Pi) ? 4 : 10;
+  L.nch = mode == kFit4Pi ? k4PiChannels : 1;
   return L;
 }
 
@@ -163,19 +180,29 @@ struct Stride2D {
   }
 };
 
-// Outputs are distributed over the lanes: lane l < NV receives gradient entry
-// l (gl) and Hessian row l (hr), or Fisher row l; err_out is on every lane.
-template <int MODE>
-__device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int lane,
-                         const float* th, bool dup45, bool FISHER, FPair& err_out, float& gl,
-                         float (&hr)[ModeTraits<MODE>::NV]) {
+// Phase position of a 4Pi channel wrapped into [1, 1 + P) by one period,
+// P = nW - 1: the phase axis of the coefficients holds one period of phase
+// samples plus one (the caller's bsarray of the phase-resolved PSF).
+__device__ __forceinline__ float wrap_phase(float w, int nw) {
+  const float P = (float)(nw - 1);
+  if (w < 1.0f) return w + P;
+  if (w >= (float)nw) return w - P;
+  return w;
+}
+
+// One image channel of one ROI evaluation: model and derivatives at th for
+// every pixel of `data`, accumulated into this lane's partial sums (err, and
+// acc = gradient 0 .. NV-1, packed Hessian or Fisher upper triangle NV ..).
+template <int MODE, int KP>
+__device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout& L, float* ws,
+                                             const float* data, int lane, const float* th,
+                                             bool dup45, bool FISHER, FPair& err,
+                                             float (&acc)[KP]) {
   using TR = ModeTraits<MODE>;
   constexpr int D = TR::D;
   constexpr int NV = TR::NV;
-  constexpr int NH = NV * (NV + 1) / 2;
   const int s = L.s;
   const ModelDev& m = a.m;
-  float* data = ws;
   int* kxs = reinterpret_cast<int*>(ws + L.off_kx());
   int* kys = reinterpret_cast<int*>(ws + L.off_ky());
   float* w = ws + L.off_w();
@@ -428,15 +455,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
   __syncwarp();
   PHASE_MARK(2);
 
-  // (C) X contraction per pixel, fused with the likelihood sums. acc holds
-  // this lane's partial gradient (0 .. NV-1) and packed Hessian or Fisher
-  // upper triangle (NV .. NV+NH-1).
-  constexpr int K = NV + NH;
-  constexpr int KP = (K + 31) / 32 * 32;
-  FPair err{0.0f, 0.0f};
-  float acc[KP];
-#pragma unroll
-  for (int k = 0; k < KP; ++k) acc[k] = 0.0f;
+  // (C) X contraction per pixel, fused with the likelihood sums.
   {
     const float bx0 = w[8], bx1 = w[9], bx2 = w[10], bx3 = w[11];
     const float dx0 = w[12], dx1 = w[13], dx2 = w[14];
@@ -546,6 +565,39 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
     }
   }
   PHASE_MARK(3);
+}
+
+// Outputs are distributed over the lanes: lane l < NV receives gradient entry
+// l (gl) and Hessian row l (hr), or Fisher row l; err_out is on every lane.
+template <int MODE>
+__device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int lane,
+                         const float* th, bool dup45, bool FISHER, FPair& err_out, float& gl,
+                         float (&hr)[ModeTraits<MODE>::NV]) {
+  using TR = ModeTraits<MODE>;
+  constexpr int NV = TR::NV;
+  constexpr int NH = NV * (NV + 1) / 2;
+  constexpr int K = NV + NH;
+  constexpr int KP = (K + 31) / 32 * 32;
+  FPair err{0.0f, 0.0f};
+  float acc[KP];
+#pragma unroll
+  for (int k = 0; k < KP; ++k) acc[k] = 0.0f;
+  if constexpr (TR::NCH == 1) {
+    channel_pass<MODE, KP>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc);
+  } else {
+    // 4Pi: channel c sees the shared parameters plus its offsets dT[c], with
+    // its phase shifted by shift[c] and wrapped; the sums run over all
+    // channels' pixels.
+    const float* dts = ws + L.off_dt();
+    for (int ch = 0; ch < TR::NCH; ++ch) {
+      float thc[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) thc[k] = th[k] + dts[ch * NV + k];
+      thc[5] = wrap_phase(thc[5] + a.m.shift[ch], a.m.n[3]);
+      channel_pass<MODE, KP>(a, L, ws, ws + ch * L.s2p, lane, thc, false, FISHER, err, acc);
+    }
+  }
+  PHASE_DECL();
   // Reduce-scatter: lane t gets the total of value t (and t + 32).
   float t0, t1 = 0.0f;
   {
@@ -643,6 +695,9 @@ __device__ __forceinline__ void clamp_fade(int l, float& c, float& f) {
   } else if (MODE == 7) {
     c = (l < 2) ? 1.0f : (l == 2) ? 10000.0f : (l == 3) ? 20.0f : (l == 4) ? 2.0f : 0.00001f;
     f = (l < 2) ? 0.5f : (l == 2) ? 0.4f : (l == 3) ? 0.5f : (l == 4) ? 0.7f : 0.8f;
+  } else if (MODE == kFit4Pi) {
+    c = (l < 2) ? 1.0f : (l == 2) ? 10000.0f : (l == 3) ? 20.0f : 2.0f;
+    f = 0.5f;
   } else {
     c = (l < 2) ? 1.0f : (l == 2) ? 10000.0f : (l == 3) ? 20.0f : (l < 7) ? 2.0f : 0.1f;
     f = 0.5f;
@@ -671,75 +726,119 @@ __device__ __forceinline__ float lane_solve(int lane, const float (&lr)[NV], con
   return x;
 }
 
+// Stage one ROI in the warp's shared memory: its pixels (4Pi: the four
+// channel planes, rois laid out [channel][roi][s][s]) and the 4Pi channel
+// offsets dT [roi][channel][6].
+template <int MODE>
+__device__ __forceinline__ void load_roi(const FitArgs& a, const WarpLayout& L, float* ws,
+                                         int lane, int64_t roi) {
+  const int s2 = L.s * L.s;
+  const int nch = ModeTraits<MODE>::NCH;
+  for (int ch = 0; ch < nch; ++ch) {
+    const float* src = a.rois + ((int64_t)ch * a.nfits + roi) * (int64_t)s2;
+    float* dst = ws + ch * L.s2p;
+    for (int p = lane; p < s2; p += 32) dst[p] = __ldg(src + p);
+  }
+  if constexpr (ModeTraits<MODE>::NCH > 1) {
+    constexpr int ND = ModeTraits<MODE>::NCH * ModeTraits<MODE>::NV;
+    if (lane < ND) ws[L.off_dt() + lane] = a.dT ? __ldg(a.dT + roi * ND + lane) : 0.0f;
+  }
+  __syncwarp();
+}
+
+// Initial x, y, N, bg of one image (CPUgaussLib.cpp:172-225 centroid and
+// max / min, CPUmleFit_LM.cpp:2477-2482), warp-uniform in g.
+__device__ __forceinline__ void initial_guess(const float* data, int s, int lane, float (&g)[4]) {
+  const int s2 = s * s;
+  FPair tx{0.f, 0.f}, ty{0.f, 0.f}, ts{0.f, 0.f};
+  float mx = 0.0f, mn = 10e10f;
+  bool nan_seen = false;
+  Stride2D ix(lane, s);
+  for (int p = lane; p < s2; p += 32, ix.next()) {
+    float d = data[p];
+    const int jj = ix.r, ii = ix.c;
+    tx.add(d * (float)ii);
+    ty.add(d * (float)jj);
+    ts.add(d);
+    nan_seen |= (d != d);
+    mx = (mx > d) ? mx : d;
+    mn = (mn < d) ? mn : d;
+  }
+  tx = warp_sum_pair(tx);
+  ty = warp_sum_pair(ty);
+  ts = warp_sum_pair(ts);
+  const float tsum = ts.hi + ts.lo;
+  if (__any_sync(kFull, nan_seen)) {
+    // The reference's max/min fold is order dependent with NaN pixels:
+    // replay it sequentially.
+    mx = 0.0f;
+    mn = 10e10f;
+    for (int p0 = 0; p0 < s2; ++p0) {
+      const float d = data[p0];
+      mx = (mx > d) ? mx : d;
+      mn = (mn < d) ? mn : d;
+    }
+  } else {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+      mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
+    }
+  }
+  // N0 = max(0, (max - min) * 2 * pi * 1.5 * 1.5), bg0 = max(min, 0.01),
+  // evaluated in double as in the reference's expression.
+  const double n0 = ((double)mx - (double)mn) * 2.0 * (double)3.141592f * 1.5 * 1.5;
+  g[0] = (tx.hi + tx.lo) / tsum;
+  g[1] = (ty.hi + ty.lo) / tsum;
+  g[2] = (float)((0.0 > n0) ? 0.0 : n0);
+  g[3] = (mn > 0.01f) ? mn : 0.01f;
+}
+
 template <int MODE>
 __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int lane, int64_t roi) {
   using TR = ModeTraits<MODE>;
   constexpr int NV = TR::NV;
-  constexpr int NH = NV * (NV + 1) / 2;
   const int s = L.s;
-  const int s2 = s * s;
-  float* data = ws;
-  const float* src = a.rois + roi * (int64_t)s2;
-  for (int p = lane; p < s2; p += 32) data[p] = __ldg(src + p);
-  __syncwarp();
+  load_roi<MODE>(a, L, ws, lane, roi);
 
   PHASE_DECL();
   // Initial guesses (CPUgaussLib.cpp:172-225, CPUmleFit_LM.cpp:2477-2482),
   // then lane l keeps parameter l.
   float par;
   {
-    FPair tx{0.f, 0.f}, ty{0.f, 0.f}, ts{0.f, 0.f};
-    float mx = 0.0f, mn = 10e10f;
-    bool nan_seen = false;
-    Stride2D ix(lane, s);
-    for (int p = lane; p < s2; p += 32, ix.next()) {
-      float d = data[p];
-      const int jj = ix.r, ii = ix.c;
-      tx.add(d * (float)ii);
-      ty.add(d * (float)jj);
-      ts.add(d);
-      nan_seen |= (d != d);
-      mx = (mx > d) ? mx : d;
-      mn = (mn < d) ? mn : d;
-    }
-    tx = warp_sum_pair(tx);
-    ty = warp_sum_pair(ty);
-    ts = warp_sum_pair(ts);
-    const float tsum = ts.hi + ts.lo;
-    if (__any_sync(kFull, nan_seen)) {
-      // The reference's max/min fold is order dependent with NaN pixels:
-      // replay it sequentially.
-      mx = 0.0f;
-      mn = 10e10f;
-      for (int p0 = 0; p0 < s2; ++p0) {
-        const float d = data[p0];
-        mx = (mx > d) ? mx : d;
-        mn = (mn < d) ? mn : d;
-      }
-    } else {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
-        mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
-      }
-    }
-    // N0 = max(0, (max - min) * 2 * pi * 1.5 * 1.5), bg0 = max(min, 0.01),
-    // evaluated in double as in the reference's expression.
-    const double n0 = ((double)mx - (double)mn) * 2.0 * (double)3.141592f * 1.5 * 1.5;
     float v = 0.0f;
-    if (lane == 0) v = (tx.hi + tx.lo) / tsum;
-    if (lane == 1) v = (ty.hi + ty.lo) / tsum;
-    if (lane == 2) v = (float)((0.0 > n0) ? 0.0 : n0);
-    if (lane == 3) v = (mn > 0.01f) ? mn : 0.01f;
+    if constexpr (TR::NCH == 1) {
+      float g[4];
+      initial_guess(ws, s, lane, g);
+      if (lane < 4) v = g[lane];
+    } else {
+      // 4Pi: the mean over the channels of the single-channel rule, the
+      // centroid taken back by the channel's offset.
+      const float* dts = ws + L.off_dt();
+      float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int ch = 0; ch < TR::NCH; ++ch) {
+        float g[4];
+        initial_guess(ws + ch * L.s2p, s, lane, g);
+        sum[0] += g[0] - dts[ch * NV + 0];
+        sum[1] += g[1] - dts[ch * NV + 1];
+        sum[2] += g[2];
+        sum[3] += g[3];
+      }
+      if (lane < 4) v = sum[lane] / (float)TR::NCH;
+    }
     if (MODE == 6) {
       if (lane == 4) v = (float)a.m.n[2] / 2.0f;
     } else if (MODE == 7) {
       const bool use = a.m.init_p_len >= 2 && a.m.init_p[0] != 0.0f;
       if (lane == 4) v = use ? a.m.init_p[0] : (float)a.m.n[2] / 2.0f;
       if (lane == 5) v = use ? a.m.init_p[1] : (float)a.m.n[3] / 2.0f;
-    } else {
+    } else if (MODE == 8) {
       // (z, w, u, g2) from initP, shared by all ROIs (CPUmleFit_LM.cpp:3246-3256)
       if (lane >= 4 && lane < 8) v = a.m.init_p[lane - 4];
+    } else {
+      // 4Pi: per-ROI initial z and phase
+      if (lane == 4) v = a.z0[roi];
+      if (lane == 5) v = wrap_phase(a.w0[roi], a.m.n[3]);
     }
     par = v;
   }
@@ -945,6 +1044,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
         const float wmax = (float)a.m.n[3] - 0.5f;
         par = (par < wmax) ? par : wmax;
       }
+      if (MODE == kFit4Pi && lane == 5) par = wrap_phase(par, a.m.n[3]);
       if (MODE == 8) {
         if (lane == 5) {
           // periodic azimuth (:3436-3443): period nW - 2
@@ -1181,10 +1281,8 @@ __global__ void __launch_bounds__(128) eval_kernel(FitArgs a, const float* theta
   const int wpb = blockDim.x >> 5;
   float* ws = smem + wib * L.total();
   const int64_t total_warps = (int64_t)gridDim.x * wpb;
-  const int s2 = a.s * a.s;
   for (int64_t roi = (int64_t)blockIdx.x * wpb + wib; roi < a.nfits; roi += total_warps) {
-    for (int p = lane; p < s2; p += 32) ws[p] = __ldg(a.rois + roi * (int64_t)s2 + p);
-    __syncwarp();
+    load_roi<MODE>(a, L, ws, lane, roi);
     float th[NV];
 #pragma unroll
     for (int i = 0; i < NV; ++i) th[i] = theta[i * a.nfits + roi];
@@ -1215,6 +1313,7 @@ cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fi
   if (mode == 6) kern = eval_kernel<6>;
   else if (mode == 7) kern = eval_kernel<7>;
   else if (mode == 8) kern = eval_kernel<8>;
+  else if (mode == kFit4Pi) kern = eval_kernel<kFit4Pi>;
   else return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
@@ -1283,6 +1382,7 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
   if (mode == 6) kern = fit_kernel<6>;
   else if (mode == 7) kern = fit_kernel<7>;
   else if (mode == 8) kern = fit_kernel<8>;
+  else if (mode == kFit4Pi) kern = fit_kernel<kFit4Pi>;
   else return cudaErrorInvalidValue;
   // Warps per block: the choice among 4, 2, 1 that keeps the most warps
   // resident per SM (shared memory per warp grows with s and the model).

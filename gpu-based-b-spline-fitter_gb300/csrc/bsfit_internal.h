@@ -6,9 +6,14 @@
 
 namespace bsfit {
 
+// Model tag of the four-channel 4Pi fit (the reference's separate
+// GPUmleFit_LM_4Pi_bspline entry, which has no fit-type number).
+constexpr int kFit4Pi = 9;
+constexpr int k4PiChannels = 4;
+
 // A PSF model resident on the device.
 struct ModelDev {
-  int fittype;           // 6, 7, 8
+  int fittype;           // 6, 7, 8, or kFit4Pi
   const float* coeff;    // device
   const float* coeff3;   // device (fit type 8)
   int cd[5];             // coefficient sizes, MATLAB order (Y, X, Z, W, U)
@@ -18,6 +23,7 @@ struct ModelDev {
   int n[5];
   float init_p[4];
   int init_p_len;
+  float shift[4];        // 4Pi models: per-channel phase shifts (knot units)
 };
 
 struct FitArgs {
@@ -36,6 +42,11 @@ struct FitArgs {
   float* trace;
   int trace_max;
   int flags;
+  // 4Pi only: per-ROI channel offsets dT [nfits][4][6], initial z and phase
+  // [nfits]; rois holds [4][nfits][s][s].
+  const float* dT;
+  const float* z0;
+  const float* w0;
 };
 
 constexpr int TRACE_REC = 32;

@@ -57,7 +57,9 @@ typedef enum bsfit_status {
   /* a bounded device-side wait ran out (batched / serving forms) */
   BSFIT_E_TIMEOUT = 12,
   /* more segments than the allocation-free entry point's fixed scratch holds */
-  BSFIT_E_STATIC_LIMIT = 13
+  BSFIT_E_STATIC_LIMIT = 13,
+  /* 4Pi fit with unshared parameters, or a channel count other than 4 */
+  BSFIT_E_UNSHARED = 14
 } bsfit_status;
 
 /* Human-readable text of a status code (replaces mexErrMsgIdAndTxt texts). */
@@ -245,6 +247,59 @@ int bsfit_server_reset_stats(bsfit_server server);
  */
 #define BSFIT_STATIC_MAX_SEGMENTS 48
 int bsfit_batch_fit_device_static(const bsfit_segment* segs, int32_t nseg, void* stream);
+
+/*
+ * 4Pi fit: four interference channels of one emitter fitted with shared
+ * parameters (x, y, N, bg, z, phase; NV = 6) against one 4D (x, y, z, phase)
+ * B-spline. Replaces GPUmleFit_LM_4Pi_bspline, which the reference ships only
+ * as a compiled mex; its interface is taken from the caller,
+ * demo_4pi/bspline_based_4piloc_v4.m:196-216:
+ *
+ *   [P, CRLB, LL] = GPUmleFit_LM_4Pi_bspline(imstack, shared, iterations,
+ *                        coeff, dT, initZ, initPhi, phase_shift)
+ *
+ * imstack: [s, s, N, 4] (channel slowest). shared: 6 flags, all 1 (the only
+ *   setting any reference caller uses; others give BSFIT_E_UNSHARED).
+ * coeff: the bsarray of the phase-resolved PSF, dims (Y, X, Z, W) with the
+ *   phase samples covering one period plus one (the period is W - 4 knots,
+ *   bspline_based_4piloc_v4.m:80-88).
+ * dT: [6, 4, N] per-ROI per-channel parameter offsets (channel c is evaluated
+ *   at theta + dT[:, c, n]). initZ, initPhi: [N] initial z and phase, in knot
+ *   units. phase_shift: [4] per-channel phase shifts in knot units.
+ * P: [N x 7] (last column = iterations; the phase column is in knots,
+ *   [1, 1 + period)), CRLB: [N x 6], LL: [N].
+ * The method (the LM machinery of fit type 7 without its quirks, all channels'
+ * pixels in one likelihood) is this library's restatement; with the source of
+ * the reference's 4Pi fitter absent, parity with it is not pinned.
+ */
+#define BSFIT_FITTYPE_4PI 9  /* model tag of 4Pi models (not a reference fit type) */
+#define BSFIT_4PI_CHANNELS 4
+int bsfit_GPUmleFit_LM_4Pi_bspline(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                                   int64_t nfits, int64_t n_channels, const uint32_t* shared,
+                                   int64_t shared_numel, int32_t iterations, const float* coeff,
+                                   int32_t coeff_ndim, const int64_t* coeff_dims, const float* dT,
+                                   int64_t dT_numel, const float* initZ, int64_t initZ_numel,
+                                   const float* initPhi, int64_t initPhi_numel,
+                                   const float* phase_shift, int64_t phase_shift_numel,
+                                   int32_t silent, float* P, float* CRLB, float* LL);
+
+/* Device-resident 4Pi model: 4D coefficients and the channels' phase shifts. */
+int bsfit_model_create_4pi(const float* coeff, int32_t coeff_ndim, const int64_t* coeff_dims,
+                           const float* phase_shift, int32_t n_channels, bsfit_model* out);
+
+/* Asynchronous 4Pi fit with device pointers: d_rois [4][nfits][s][s],
+ * d_dT [nfits][4][6] (NULL = no offsets), d_initZ / d_initPhi [nfits]; outputs
+ * as for bsfit_fit_device with NV = 6. */
+int bsfit_fit4pi_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                        int32_t iterations, const float* d_dT, const float* d_initZ,
+                        const float* d_initPhi, float* d_P, float* d_CRLB, float* d_LL,
+                        void* stream);
+
+/* One 4Pi likelihood evaluation per ROI at given parameters (d_theta [6][nfits]);
+ * d_out as for bsfit_eval_device with NV = 6. */
+int bsfit_eval4pi_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                         const float* d_dT, const float* d_theta, int32_t fisher, float* d_out,
+                         void* stream);
 
 #ifdef __cplusplus
 }

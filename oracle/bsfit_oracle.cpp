@@ -1042,3 +1042,250 @@ void oracle_eval8_f64(const double* rois, const double* coeff5, const double* co
   eval8(rois, coeff5, coeff3, dims, sz, nfits, theta, fisher, out);
 }
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// 4Pi fit (four interference channels, shared parameters).
+//
+// The reference ships this fitter only as a compiled binary; its source is not
+// part of the reference. The method below is restated from what the reference
+// does publish: the call (demo_4pi/bspline_based_4piloc_v4.m:196-214:
+// imstack [s, s, N, 4], shared flags, 100 iterations, the 4D (x, y, z, phase)
+// coefficients, per-ROI per-channel parameter offsets dT [NV, 4, N], initial z
+// and phase per ROI, per-channel phase shifts, phase in knot units with the
+// +1 knot convention, :216), the forward model of one channel
+// (demo_4pi/store/simBSplinePSF.m:15-61: the 4D spline at the channel's
+// position with the phase shifted by the channel's phase shift and wrapped to
+// one period) and the LM machinery of the other B-spline fit types. The
+// coefficient array is the caller's bsarray of the phase-resolved PSF
+// (bspline_based_4piloc_v4.m:80-88: samples at phases 0 .. (nPhi) dphi with
+// 2 pi at sample nPhi - 1), so one period spans P = nW - 1 knots (nW = the
+// array's phase size - 3) and a phase position lives in [1, 1 + P).
+// The choices that are this implementation's own: all six parameters shared
+// (the demo's shared = [1 1 1 1 1 1]), channel c evaluated at theta + dT[c]
+// with its phase shifted by shift[c]; clamps {1, 1, 1e4, 20, 2, 2} with fade
+// 0.5; initial x, y, N, bg the mean over channels of the single-channel rule
+// (x, y corrected by the channel's offset); bounds N >= 1, bg >= 0.01,
+// 0 <= z <= nZ - 0.5; the phase parameter and each channel's shifted phase
+// wrapped into [1, 1 + P) one period at a time.
+// THIS DEFINES THE METHOD: parity for it is not pinned to a reference.
+
+namespace {
+
+// Wrap of a phase position into [1, 1 + P), P = nW - 1, by one period.
+template <typename T>
+inline T wrap_phase(T w, int nw) {
+  const T P = (T)(nw - 1);
+  if (w < (T)1) return w + P;
+  if (w >= (T)nw) return w - P;
+  return w;
+}
+
+template <typename T>
+struct Model4Pi {
+  static constexpr int NV = 6;
+  static constexpr int C = 4;
+  const T* coeff;
+  int n[4];
+  const T* dT;        // [C][NV] offsets of this ROI
+  T shift[C];         // per-channel phase shifts (knot units)
+  Model4D<T>* ch[C];  // per-channel 4D evaluators (weights per channel)
+  void prepare(const T* theta, int sz) {
+    for (int c = 0; c < C; ++c) {
+      T tc[NV];
+      for (int t = 0; t < NV; ++t) tc[t] = theta[t] + dT[c * NV + t];
+      tc[5] = wrap_phase<T>(tc[5] + shift[c], n[3]);
+      ch[c]->prepare(tc, sz);
+    }
+  }
+  // model and dudt of channel c at pixel (ii, jj)
+  void pixel(int c, int ii, int jj, const T* theta, T* dudt, T* model) const {
+    T tc[NV];
+    for (int t = 0; t < NV; ++t) tc[t] = theta[t] + dT[c * NV + t];
+    ch[c]->pixel(ii, jj, tc, dudt, model);
+  }
+};
+
+template <typename T>
+void eval_4pi(Model4Pi<T>& mdl, int sz, const T* const* planes, const T* theta, bool fisher,
+              T* err, T* jac, T* hes) {
+  constexpr int NV = 6;
+  *err = 0;
+  for (int i = 0; i < NV; ++i) jac[i] = 0;
+  for (int i = 0; i < NV * NV; ++i) hes[i] = 0;
+  mdl.prepare(theta, sz);
+  for (int c = 0; c < Model4Pi<T>::C; ++c)
+    for (int ii = 0; ii < sz; ii++)
+      for (int jj = 0; jj < sz; jj++) {
+        T dudt[NV], model;
+        mdl.pixel(c, ii, jj, theta, dudt, &model);
+        const T data = planes[c][sz * jj + ii];
+        if (!fisher)
+          accumulate_pixel<T>(model, data, dudt, NV, true, err, jac, hes);
+        else
+          accumulate_fisher<T>(model, data, dudt, NV, hes, err);
+      }
+}
+
+template <typename T>
+void fit_4pi_roi(const T* coeff, const int* n, int sz, int nfits, int r, const T* imstack,
+                 const T* dT, const T* initZ, const T* initPhi, const T* shift, int iterations,
+                 T* P, T* CRLB, T* LL) {
+  constexpr int NV = 6, C = 4;
+  Model4D<T> chm[C];
+  Model4Pi<T> mdl;
+  mdl.coeff = coeff;
+  for (int a = 0; a < 4; ++a) mdl.n[a] = n[a];
+  mdl.dT = dT + (long long)r * C * NV;
+  for (int c = 0; c < C; ++c) {
+    mdl.shift[c] = shift[c];
+    chm[c].coeff = coeff;
+    for (int a = 0; a < 4; ++a) chm[c].n[a] = n[a];
+    chm[c].fr.off = (T)((float)(n[1] - sz) / 2.0f);
+    mdl.ch[c] = &chm[c];
+  }
+  const T* planes[C];
+  for (int c = 0; c < C; ++c) planes[c] = imstack + ((long long)c * nfits + r) * sz * sz;
+  // initial values: mean over the channels of the single-channel rule
+  // (CPUgaussLib.cpp:172-225, CPUmleFit_LM.cpp:2477-2482)
+  T th[NV], oth[NV];
+  {
+    T sx = 0, sy = 0, sn = 0, sb = 0;
+    for (int c = 0; c < C; ++c) {
+      T t4[4];
+      initial_guess<T>(sz, planes[c], t4);
+      sx += t4[0] - mdl.dT[c * NV + 0];
+      sy += t4[1] - mdl.dT[c * NV + 1];
+      sn += t4[2];
+      sb += t4[3];
+    }
+    th[0] = sx / (T)C;
+    th[1] = sy / (T)C;
+    th[2] = sn / (T)C;
+    th[3] = sb / (T)C;
+  }
+  th[4] = initZ[r];
+  th[5] = wrap_phase<T>(initPhi[r], n[3]);
+  const T clamp0[NV] = {1, 1, 10000, 20, 2, 2};
+  T clampv[NV], oclamp[NV], sign[NV] = {0}, osign[NV] = {0}, upd[NV];
+  for (int i = 0; i < NV; ++i) clampv[i] = oclamp[i] = clamp0[i], oth[i] = th[i];
+  T lambda = 1, olambda = 1;
+  T err = 1e12, oerr = 1e13;
+  T jac[NV], hes[NV * NV], L[NV * NV], U[NV * NV];
+  eval_4pi<T>(mdl, sz, planes, th, false, &err, jac, hes);
+  int kk;
+  for (kk = 0; kk < iterations; kk++) {
+    if (std::fabs((err - oerr) / err) < kTOL) break;
+    if ((double)err > 1.5 * (double)oerr) {
+      for (int i = 0; i < NV; i++) sign[i] = osign[i], clampv[i] = oclamp[i], th[i] = oth[i];
+      lambda = olambda;
+      err = oerr;
+      lambda = 10 * lambda;
+    } else if (err < oerr) {
+      if (lambda > 1) lambda = (T)((double)lambda * 0.8);
+      else if (lambda < 1) lambda = 1;
+    }
+    for (int i = 0; i < NV; i++) hes[i * NV + i] *= lambda;
+    int info = cholesky<T>(hes, NV, L, U);
+    if (info == 0) {
+      lu_evaluate<T>(L, U, jac, NV, upd);
+      for (int i = 0; i < NV; ++i)
+        if (std::isnan(upd[i])) info = 1;
+    }
+    if (info == 0) {
+      for (int i = 0; i < NV; i++) osign[i] = sign[i], oclamp[i] = clampv[i], oth[i] = th[i];
+      olambda = lambda;
+      oerr = err;
+      for (int l = 0; l < NV; l++) {
+        if (sign[l] != 0 && ((sign[l] == 1 && upd[l] < 0) || (sign[l] == -1 && upd[l] > 0)))
+          clampv[l] = clampv[l] * (T)0.5;
+        sign[l] = (upd[l] > 0) ? 1 : -1;
+        th[l] = th[l] - upd[l] / (1 + std::fabs(upd[l] / clampv[l]));
+      }
+      th[2] = (T)mmax((double)th[2], 1.0);
+      th[3] = (T)mmax((double)th[3], 0.01);
+      th[4] = (T)mmax((double)th[4], 0.0);
+      th[4] = (T)mmin((double)th[4], (double)T(n[2]) - 0.5);
+      th[5] = wrap_phase<T>(th[5], n[3]);
+      eval_4pi<T>(mdl, sz, planes, th, false, &err, jac, hes);
+    } else {
+      lambda = 10 * lambda;
+    }
+  }
+  T M[NV * NV], Minv[NV * NV], diag[NV], Div = 0;
+  eval_4pi<T>(mdl, sz, planes, th, true, &Div, jac, M);
+  mat_inv_n<T>(M, Minv, diag, NV);
+  for (int i = 0; i < NV; i++) P[(long long)nfits * i + r] = th[i];
+  P[(long long)nfits * NV + r] = (T)kk;
+  for (int i = 0; i < NV; i++) CRLB[(long long)nfits * i + r] = diag[i];
+  LL[r] = Div;
+}
+
+template <typename T>
+void fit4pi(const T* imstack, const T* coeff, const int* cdims, int sz, int nfits, int iterations,
+            const T* dT, const T* initZ, const T* initPhi, const T* shift, T* P, T* CRLB, T* LL,
+            int threads) {
+  int n[4] = {cdims[1] - 3, cdims[0] - 3, cdims[2] - 3, cdims[3] - 3};
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads > 0 ? threads : 1)
+  for (int r = 0; r < nfits; ++r)
+    fit_4pi_roi<T>(coeff, n, sz, nfits, r, imstack, dT, initZ, initPhi, shift, iterations, P, CRLB,
+                   LL);
+}
+
+}  // namespace
+
+extern "C" {
+// 4Pi fit: imstack [C=4][N][s][s] (MATLAB [s, s, N, 4]); coeff (x, y, z, phase)
+// with dims (Y, X, Z, W); dT [N][4][6] (MATLAB [6, 4, N]); initZ, initPhi [N];
+// shift [4] (knot units). P [7][N], CRLB [6][N], LL [N].
+void oracle_fit4pi_f32(const float* imstack, const float* coeff, const int* cdims, int sz, int nfits,
+                       int iterations, const float* dT, const float* initZ, const float* initPhi,
+                       const float* shift, float* P, float* CRLB, float* LL, int threads) {
+  fit4pi<float>(imstack, coeff, cdims, sz, nfits, iterations, dT, initZ, initPhi, shift, P, CRLB,
+                LL, threads);
+}
+void oracle_fit4pi_f64(const double* imstack, const double* coeff, const int* cdims, int sz,
+                       int nfits, int iterations, const double* dT, const double* initZ,
+                       const double* initPhi, const double* shift, double* P, double* CRLB,
+                       double* LL, int threads) {
+  fit4pi<double>(imstack, coeff, cdims, sz, nfits, iterations, dT, initZ, initPhi, shift, P, CRLB,
+                 LL, threads);
+}
+}  // extern "C"
+
+extern "C" {
+// One 4Pi evaluation per ROI at given theta (6 x nfits column-major); out as
+// bsfit_eval4pi_device: value, gradient, packed upper-triangle Hessian / Fisher.
+void oracle_eval4pi_f64(const double* imstack, const double* coeff, const int* cdims, int sz,
+                        int nfits, const double* dT, const double* shift, const double* theta,
+                        int fisher, double* out) {
+  constexpr int NV = 6, C = 4, NH = NV * (NV + 1) / 2;
+  int n[4] = {cdims[1] - 3, cdims[0] - 3, cdims[2] - 3, cdims[3] - 3};
+  Model4D<double>* chm = new Model4D<double>[C];
+  for (int r = 0; r < nfits; ++r) {
+    Model4Pi<double> mdl;
+    mdl.coeff = coeff;
+    for (int a = 0; a < 4; ++a) mdl.n[a] = n[a];
+    mdl.dT = dT + (long long)r * C * NV;
+    for (int c = 0; c < C; ++c) {
+      mdl.shift[c] = shift[c];
+      chm[c].coeff = coeff;
+      for (int a = 0; a < 4; ++a) chm[c].n[a] = n[a];
+      chm[c].fr.off = (double)((float)(n[1] - sz) / 2.0f);
+      mdl.ch[c] = &chm[c];
+    }
+    const double* planes[C];
+    for (int c = 0; c < C; ++c) planes[c] = imstack + ((long long)c * nfits + r) * sz * sz;
+    double th[NV];
+    for (int i = 0; i < NV; ++i) th[i] = theta[(long long)i * nfits + r];
+    double err = 0, jac[NV], hes[NV * NV];
+    eval_4pi<double>(mdl, sz, planes, th, fisher != 0, &err, jac, hes);
+    double* o = out + (long long)r * (1 + NV + NH);
+    o[0] = err;
+    for (int i = 0; i < NV; ++i) o[1 + i] = fisher ? 0.0 : jac[i];
+    int k = 0;
+    for (int l = 0; l < NV; ++l)
+      for (int m = l; m < NV; ++m) o[1 + NV + k++] = hes[l * NV + m];
+  }
+  delete[] chm;
+}
+}  // extern "C"

@@ -154,3 +154,42 @@ def _trace(self, rois, fittype, iterations, coeff, roi, init_p=None, precision="
 
 
 Oracle.trace = _trace
+
+
+def _fit4pi(self, rois, iterations, coeff, dT, init_z, init_phi, phase_shift, precision="f64",
+            threads=1):
+    """4Pi fit (oracle_fit4pi_*): rois (4, N, s, s); dT (N, 4, 6); init_z,
+    init_phi (N,); phase_shift (4,). Returns P (N, 7), CRLB (N, 6), LL (N,)."""
+    dt = np.float32 if precision == "f32" else np.float64
+    rois = np.ascontiguousarray(rois, dtype=dt)
+    n, s = rois.shape[1], rois.shape[-1]
+    coeff = np.ascontiguousarray(coeff, dtype=dt)
+    dims = (ctypes.c_int * 4)(*reversed(coeff.shape))
+    arrs = [np.ascontiguousarray(a, dtype=dt) for a in (dT, init_z, init_phi, phase_shift)]
+    P = np.zeros((7, n), dt)
+    C = np.zeros((6, n), dt)
+    L = np.zeros(n, dt)
+    fn = getattr(self._lib, f"oracle_fit4pi_{precision}")
+    fn(_ptr(rois, dt), _ptr(coeff, dt), dims, _i(s), _i(n), _i(iterations),
+       *[_ptr(a, dt) for a in arrs], _ptr(P, dt), _ptr(C, dt), _ptr(L, dt), _i(threads))
+    return P.T.copy(), C.T.copy(), L
+
+
+def _eval4pi(self, rois, coeff, dT, phase_shift, theta, fisher=False):
+    """One 4Pi evaluation per ROI at theta ((N, 6)): (N, 28) float64 rows."""
+    rois = np.ascontiguousarray(rois, dtype=np.float64)
+    n, s = rois.shape[1], rois.shape[-1]
+    coeff = np.ascontiguousarray(coeff, dtype=np.float64)
+    dims = (ctypes.c_int * 4)(*reversed(coeff.shape))
+    d = np.ascontiguousarray(dT, dtype=np.float64)
+    ps = np.ascontiguousarray(phase_shift, dtype=np.float64)
+    th = np.ascontiguousarray(np.asarray(theta, np.float64)[:, :6].T)
+    out = np.zeros((n, 28), np.float64)
+    self._lib.oracle_eval4pi_f64(_ptr(rois, np.float64), _ptr(coeff, np.float64), dims, _i(s),
+                                 _i(n), _ptr(d, np.float64), _ptr(ps, np.float64),
+                                 _ptr(th, np.float64), _i(int(fisher)), _ptr(out, np.float64))
+    return out
+
+
+Oracle.fit4pi = _fit4pi
+Oracle.eval4pi = _eval4pi

@@ -36,8 +36,8 @@ def test_binding_matches_header():
 
 
 def test_status_strings(lib):
-    for st in range(0, 14):
-        assert lib.bsfit_status_str(st)
+    for st in range(0, 15):
+        assert lib.bsfit_status_str(st) != b"unknown status"
     assert b"square" in lib.bsfit_status_str(4)
 
 
@@ -72,3 +72,39 @@ def test_rejects_other_fittypes(fittype):
 
 def test_num_params(lib):
     assert [lib.bsfit_num_params(t) for t in (5, 6, 7, 8)] == [0, 5, 6, 8]
+
+
+def _call4pi(shared=(1, 1, 1, 1, 1, 1), channels=4, n=2, s=13, **kw):
+    import bsfit
+    im = np.zeros((channels, n, s, s), np.float32)
+    args = dict(shared=np.asarray(shared, np.uint32), iterations=100,
+                coeff=np.zeros((12, 10, 9, 9), np.float32), dT=np.zeros((n, 4, 6), np.float32),
+                initZ=np.zeros(n, np.float32), initPhi=np.ones(n, np.float32),
+                phase_shift=np.zeros(4, np.float32))
+    args.update(kw)
+    return bsfit.GPUmleFit_LM_4Pi_bspline(im, **args)
+
+
+@pytest.mark.parametrize("shared", [(1, 1, 1, 1, 1, 0), (0, 1, 1, 1, 1, 1), (1, 1, 1)])
+def test_4pi_rejects_unshared(shared):
+    import bsfit
+    with pytest.raises(bsfit.BsfitError) as e:
+        _call4pi(shared=shared)
+    assert e.value.status == 14
+
+
+def test_4pi_rejects_channel_count():
+    import bsfit
+    with pytest.raises(bsfit.BsfitError) as e:
+        _call4pi(channels=3)
+    assert e.value.status == 14
+
+
+def test_4pi_rejects_short_inputs():
+    import bsfit
+    with pytest.raises(bsfit.BsfitError) as e:
+        _call4pi(dT=np.zeros((1, 4, 6), np.float32))
+    assert e.value.status == 1
+    with pytest.raises(bsfit.BsfitError) as e:
+        _call4pi(s=52)
+    assert e.value.status == 3

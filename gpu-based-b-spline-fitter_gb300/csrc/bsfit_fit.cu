@@ -119,17 +119,17 @@ struct ModeTraits<8> {
 // the A and G maps. WP = s + 4 bounds the knot window along each lateral axis.
 struct WarpLayout {
   int s, s2p, wp, na, ng, nch;
-  __host__ __device__ int off_kx() const { return nch * s2p; }
-  __host__ __device__ int off_ky() const { return s2p + ((s + 3) & ~3); }
-  __host__ __device__ int off_w() const { return off_ky() + ((s + 3) & ~3); }
-  __host__ __device__ int off_dt() const { return off_w() + 40; }
-  __host__ __device__ int off_a() const { return off_dt() + (nch > 1 ? nch * 6 : 0); }
-  __host__ __device__ int off_g() const { return off_a() + na * wp * wp; }
-  __host__ __device__ int total() const { return off_g() + ng * wp * s; }
+  __host__ __device__ constexpr int off_kx() const { return nch * s2p; }
+  __host__ __device__ constexpr int off_ky() const { return off_kx() + ((s + 3) & ~3); }
+  __host__ __device__ constexpr int off_w() const { return off_ky() + ((s + 3) & ~3); }
+  __host__ __device__ constexpr int off_dt() const { return off_w() + 40; }
+  __host__ __device__ constexpr int off_a() const { return off_dt() + (nch > 1 ? nch * 6 : 0); }
+  __host__ __device__ constexpr int off_g() const { return off_a() + na * wp * wp; }
+  __host__ __device__ constexpr int total() const { return off_g() + ng * wp * s; }
 };
 
-__host__ __device__ inline WarpLayout make_layout(int mode, int s) {
-  WarpLayout L;
+__host__ __device__ constexpr WarpLayout make_layout(int mode, int s) {
+  WarpLayout L{};
   L.s = s;
   L.s2p = (s * s + 3) & ~3;
   L.wp = s + 4;
@@ -138,6 +138,24 @@ __host__ __device__ inline WarpLayout make_layout(int mode, int s) {
   L.nch = mode == kFit4Pi ? k4PiChannels : 1;
   return L;
 }
+
+// Every region of the layout starts after the previous one ends (pixels
+// nch * s^2, knots s each, weights 5 axes x 8, offsets nch x 6, maps), for
+// every model and ROI size.
+constexpr bool layouts_disjoint() {
+  const int modes[4] = {6, 7, 8, kFit4Pi};
+  for (int mi = 0; mi < 4; ++mi)
+    for (int s = 1; s <= 51; ++s) {
+      const WarpLayout L = make_layout(modes[mi], s);
+      if (L.nch * s * s > L.off_kx() || L.off_kx() + s > L.off_ky() ||
+          L.off_ky() + s > L.off_w() || L.off_w() + 5 * 8 > L.off_dt() ||
+          L.off_dt() + (L.nch > 1 ? L.nch * 6 : 0) > L.off_a() ||
+          L.off_a() + L.na * L.wp * L.wp > L.off_g() || L.off_g() + L.ng * L.wp * s > L.total())
+        return false;
+    }
+  return true;
+}
+static_assert(layouts_disjoint(), "per-warp shared-memory regions overlap");
 
 int warp_smem_floats(int mode, int s) { return make_layout(mode, s).total(); }
 

@@ -118,7 +118,7 @@ int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
                        bsfit_model* out);
 int bsfit_model_release(bsfit_model model);
 
-/* Fit type of a model (6, 7, 8), 0 for NULL. */
+/* Fit type of a model (6, 7, 8; BSFIT_FITTYPE_4PI for 4Pi models), 0 for NULL. */
 int32_t bsfit_model_fittype(bsfit_model model);
 
 /*

@@ -984,8 +984,10 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
         ok = false;
         break;
       }
-      const float ljj = sqrtf(ajj);
-      const float inv = 1.0f / ljj;
+      // 1/sqrt by the hardware reciprocal square root: the refinement step
+      // below absorbs its rounding (the refined steps are unchanged on 3D).
+      const float inv = rsqrtf(ajj);
+      const float ljj = ajj * inv;
       const float lij = (lane > j) ? am[j] * inv : ((lane == j) ? ljj : 0.0f);
       lr[j] = lij;
       if (lane == j) invd = inv;
@@ -1139,8 +1141,8 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     for (int j = 0; j < NV; ++j) {
       const float ajj = bcast(mr[j], j);
       if (!(ajj > 0.0f)) okc = false;
-      const float ljj = sqrtf(ajj);
-      const float inv = 1.0f / ljj;
+      const float inv = rsqrtf(ajj);
+      const float ljj = ajj * inv;
       const float lij = (lane > j) ? mr[j] * inv : ((lane == j) ? ljj : 0.0f);
       lr[j] = lij;
       if (lane == j) invd = inv;

@@ -38,11 +38,13 @@
 #include "bsfit_device.cuh"
 #include "bsfit_internal.h"
 
-// Minimum resident blocks per SM requested for the 3D kernels (4 warps each):
-// trades registers for occupancy.
+// Minimum resident blocks of 4 warps per SM requested per model: trades
+// registers for occupancy (measured: 6 blocks for 3D at 85 registers, 4 for
+// the 4D and 4Pi models at 128, 3 for the 5D model at 168 without spills).
 #ifndef BSFIT_MINBLOCKS6
-#define BSFIT_MINBLOCKS6 5
+#define BSFIT_MINBLOCKS6 6
 #endif
+#define BSFIT_MINBLOCKS(MODE) ((MODE) == 6 ? BSFIT_MINBLOCKS6 : (MODE) == 8 ? 3 : 4)
 
 namespace bsfit {
 
@@ -116,16 +118,38 @@ struct ModeTraits<8> {
 
 // Per-warp shared-memory layout (floats): the ROI's pixels (one plane per
 // channel), the per-pixel knots, the 1-D weights, the 4Pi channel offsets, and
-// the A and G maps. WP = s + 4 bounds the knot window along each lateral axis.
+// the maps. WP = s + 4 bounds the knot window along each lateral axis.
+//
+// The stage-A maps (NA per lateral node) and the stage-B maps (NG per X node
+// and pixel row) are both stored by X node ("column"): A column xr holds
+// NA x WP floats, G column xr holds NG x s. For the 5D model, whose maps
+// would otherwise bound the warps per SM by shared memory, the two share one
+// region: stage B reads only A column xr to write G column xr and walks the
+// columns in order, so G is written over A columns already consumed. With G
+// at the start of the region and A at offset a_rel with
+// (xr + 1) * GS <= a_rel + xr * AS for every column, a G column never reaches
+// an A column that is still to be read (the reads and writes of one pass of
+// the warp are separated by __syncwarp). The other models keep the two map
+// sets apart (a_rel = WP * GS) and write G without that synchronisation.
 struct WarpLayout {
   int s, s2p, wp, na, ng, nch;
+  bool alias;
+  __host__ __device__ constexpr int as() const { return na * wp; }  // A column stride
+  __host__ __device__ constexpr int gs() const { return ng * s; }   // G column stride
   __host__ __device__ constexpr int off_kx() const { return nch * s2p; }
   __host__ __device__ constexpr int off_ky() const { return off_kx() + ((s + 3) & ~3); }
   __host__ __device__ constexpr int off_w() const { return off_ky() + ((s + 3) & ~3); }
   __host__ __device__ constexpr int off_dt() const { return off_w() + 40; }
-  __host__ __device__ constexpr int off_a() const { return off_dt() + (nch > 1 ? nch * 6 : 0); }
-  __host__ __device__ constexpr int off_g() const { return off_a() + na * wp * wp; }
-  __host__ __device__ constexpr int total() const { return off_g() + ng * wp * s; }
+  __host__ __device__ constexpr int off_maps() const { return off_dt() + (nch > 1 ? nch * 6 : 0); }
+  __host__ __device__ constexpr int a_rel() const {
+    return alias ? gs() + (wp - 1) * (gs() > as() ? gs() - as() : 0) : wp * gs();
+  }
+  __host__ __device__ constexpr int off_g() const { return off_maps(); }
+  __host__ __device__ constexpr int off_a() const { return off_maps() + a_rel(); }
+  __host__ __device__ constexpr int maps_size() const {
+    return (a_rel() + wp * as() > wp * gs()) ? a_rel() + wp * as() : wp * gs();
+  }
+  __host__ __device__ constexpr int total() const { return off_maps() + maps_size(); }
 };
 
 __host__ __device__ constexpr WarpLayout make_layout(int mode, int s) {
@@ -136,12 +160,14 @@ __host__ __device__ constexpr WarpLayout make_layout(int mode, int s) {
   L.na = mode == 6 ? 2 : (mode == 7 || mode == kFit4Pi) ? 3 : 8;
   L.ng = mode == 6 ? 3 : (mode == 7 || mode == kFit4Pi) ? 4 : 10;
   L.nch = mode == kFit4Pi ? k4PiChannels : 1;
+  L.alias = mode == 8;
   return L;
 }
 
-// Every region of the layout starts after the previous one ends (pixels
-// nch * s^2, knots s each, weights 5 axes x 8, offsets nch x 6, maps), for
-// every model and ROI size.
+// Every region starts after the previous one ends (pixels nch * s^2, knots s
+// each, weights 5 axes x 8, offsets nch x 6, maps), both map sets fit in the
+// maps region, and the aliasing rule above holds for every column, for every
+// model and ROI size.
 constexpr bool layouts_disjoint() {
   const int modes[4] = {6, 7, 8, kFit4Pi};
   for (int mi = 0; mi < 4; ++mi)
@@ -149,9 +175,11 @@ constexpr bool layouts_disjoint() {
       const WarpLayout L = make_layout(modes[mi], s);
       if (L.nch * s * s > L.off_kx() || L.off_kx() + s > L.off_ky() ||
           L.off_ky() + s > L.off_w() || L.off_w() + 5 * 8 > L.off_dt() ||
-          L.off_dt() + (L.nch > 1 ? L.nch * 6 : 0) > L.off_a() ||
-          L.off_a() + L.na * L.wp * L.wp > L.off_g() || L.off_g() + L.ng * L.wp * s > L.total())
+          L.off_dt() + (L.nch > 1 ? L.nch * 6 : 0) > L.off_maps() ||
+          L.off_a() + L.wp * L.as() > L.total() || L.off_g() + L.wp * L.gs() > L.total())
         return false;
+      for (int c = 0; c < L.wp; ++c)
+        if ((c + 1) * L.gs() > L.a_rel() + c * L.as()) return false;
     }
   return true;
 }
@@ -224,9 +252,10 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
   int* kxs = reinterpret_cast<int*>(ws + L.off_kx());
   int* kys = reinterpret_cast<int*>(ws + L.off_ky());
   float* w = ws + L.off_w();
-  float* A = ws + L.off_a();
-  float* G = ws + L.off_g();
+  float* A = ws + L.off_a();  // A[xr * AS + map * wp + yr]
+  float* G = ws + L.off_g();  // G[xr * GS + map * s + py]
   const int wp = L.wp;
+  const int AS = L.as(), GS = L.gs();
   __syncwarp();  // the previous evaluation's readers of kxs / w / G are done
   PHASE_DECL();
 
@@ -298,8 +327,8 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         float c0 = __ldg(p), c1 = __ldg(p + sz_), c2 = __ldg(p + 2 * sz_), c3 = __ldg(p + 3 * sz_);
         float v = c0 * bz0 + c1 * bz1 + c2 * bz2 + c3 * bz3;
         float dz = (c1 - c0) * dz0 + (c2 - c1) * dz1 + (c3 - c2) * dz2;
-        A[xr * wp + yr] = v;
-        A[wp * wp + xr * wp + yr] = dz;
+        A[xr * AS + yr] = v;
+        A[xr * AS + wp + yr] = dz;
       }
     } else if constexpr (D == 4) {
       const float* ww = w + 3 * 8;
@@ -322,9 +351,9 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         float v = vz[0] * bw[0] + vz[1] * bw[1] + vz[2] * bw[2] + vz[3] * bw[3];
         float dz = dzv[0] * bw[0] + dzv[1] * bw[1] + dzv[2] * bw[2] + dzv[3] * bw[3];
         float dwv = (vz[1] - vz[0]) * dw[0] + (vz[2] - vz[1]) * dw[1] + (vz[3] - vz[2]) * dw[2];
-        A[xr * wp + yr] = v;
-        A[wp * wp + xr * wp + yr] = dz;
-        A[2 * wp * wp + xr * wp + yr] = dwv;
+        A[xr * AS + yr] = v;
+        A[xr * AS + wp + yr] = dz;
+        A[xr * AS + 2 * wp + yr] = dwv;
       }
     } else {
       // 5D (z, w, u) for the mixture's 5D part, plus its 3D part (z only, on
@@ -370,7 +399,6 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
                           (int64_t)(ku - 1) * su_;
       const float* base3 = m.coeff3 + (int64_t)(kz - 1) * sz_;
       Stride2D ix(lane, wy);
-      const int ws2 = wp * wp;
       for (int t = lane; t < nodes; t += 32, ix.next()) {
         const int xr = ix.r, yr = ix.c;
         const int64_t lat = (int64_t)(xb + xr) * m.st[1] + (yb + yr);
@@ -414,59 +442,70 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         qu *= du[2];
         const float* p3 = base3 + lat;
         float e0 = __ldg(p3), e1 = __ldg(p3 + sz_), e2 = __ldg(p3 + 2 * sz_), e3 = __ldg(p3 + 3 * sz_);
-        const int o = xr * wp + yr;
-        A[o] = v;
-        A[ws2 + o] = dzv;
-        A[2 * ws2 + o] = dwv;
-        A[3 * ws2 + o] = duv;
-        A[4 * ws2 + o] = qz;
-        A[5 * ws2 + o] = qu;
-        A[6 * ws2 + o] = e0 * bz0 + e1 * bz1 + e2 * bz2 + e3 * bz3;
-        A[7 * ws2 + o] = (e1 - e0) * dz0 + (e2 - e1) * dz1 + (e3 - e2) * dz2;
+        float* o = A + xr * AS + yr;
+        o[0] = v;
+        o[wp] = dzv;
+        o[2 * wp] = dwv;
+        o[3 * wp] = duv;
+        o[4 * wp] = qz;
+        o[5 * wp] = qu;
+        o[6 * wp] = e0 * bz0 + e1 * bz1 + e2 * bz2 + e3 * bz3;
+        o[7 * wp] = (e1 - e0) * dz0 + (e2 - e1) * dz1 + (e3 - e2) * dz2;
       }
     }
   }
   __syncwarp();
   PHASE_MARK(1);
 
-  // (B) Y contraction for every (X node, pixel row ii).
+  // (B) Y contraction for every (X node, pixel row ii), column by column. For
+  // the 5D model G is written over the A columns already read (the layout's
+  // aliasing rule), so every pass of the warp reads its A values,
+  // synchronises, then writes.
   {
     const float by0 = w[0], by1 = w[1], by2 = w[2], by3 = w[3];
     const float dy0 = w[4], dy1 = w[5], dy2 = w[6];
+    constexpr int NG = TR::NG;
     const int items = wx * s;
-    const int gstride = wp * s;
     Stride2D ix(lane, s);
-    for (int t = lane; t < items; t += 32, ix.next()) {
+    for (int t0 = 0; t0 < items; t0 += 32, ix.next()) {
+      const bool act = t0 + lane < items;
       const int xr = ix.r, py = ix.c;
-      int oy = min(max(kys[py] - 1 - yb, 0), wy - 4);
-      const float* a0 = A + xr * wp + oy;
-      float v0 = a0[0], v1 = a0[1], v2 = a0[2], v3 = a0[3];
-      G[xr * s + py] = v0 * by0 + v1 * by1 + v2 * by2 + v3 * by3;
-      G[gstride + xr * s + py] = (v1 - v0) * dy0 + (v2 - v1) * dy1 + (v3 - v2) * dy2;
-      if constexpr (MODE != 8) {
+      float gv[NG];
+      if (act) {
+        const int oy = min(max(kys[py] - 1 - yb, 0), wy - 4);
+        const float* a0 = A + xr * AS + oy;
+        const float v0 = a0[0], v1 = a0[1], v2 = a0[2], v3 = a0[3];
+        gv[0] = v0 * by0 + v1 * by1 + v2 * by2 + v3 * by3;
+        gv[1] = (v1 - v0) * dy0 + (v2 - v1) * dy1 + (v3 - v2) * dy2;
+        if constexpr (MODE != 8) {
 #pragma unroll
-        for (int c = 1; c < TR::NA; ++c) {
-          const float* ac = a0 + c * wp * wp;
-          G[(c + 1) * gstride + xr * s + py] = ac[0] * by0 + ac[1] * by1 + ac[2] * by2 + ac[3] * by3;
-        }
-      } else {
-        const int ws2 = wp * wp;
-        const int o = xr * s + py;
+          for (int c = 1; c < TR::NA; ++c) {
+            const float* ac = a0 + c * wp;
+            gv[c + 1] = ac[0] * by0 + ac[1] * by1 + ac[2] * by2 + ac[3] * by3;
+          }
+        } else {
 #pragma unroll
-        for (int c = 1; c <= 3; ++c) {  // d/dz, d/dw, d/du of the 5D spline
-          const float* ac = a0 + c * ws2;
-          G[(c + 1) * gstride + o] = ac[0] * by0 + ac[1] * by1 + ac[2] * by2 + ac[3] * by3;
+          for (int c = 1; c <= 3; ++c) {  // d/dz, d/dw, d/du of the 5D spline
+            const float* ac = a0 + c * wp;
+            gv[c + 1] = ac[0] * by0 + ac[1] * by1 + ac[2] * by2 + ac[3] * by3;
+          }
+          const float* qz = a0 + 4 * wp;  // lateral side 2: offsets +1, +2
+          gv[5] = qz[2] * by2 + qz[3] * by3;
+          const float* qu = a0 + 5 * wp;  // lateral side 1: offsets -1, 0
+          gv[6] = qu[0] * by0 + qu[1] * by1;
+          const float* b3 = a0 + 6 * wp;  // 3D spline value
+          const float u0 = b3[0], u1 = b3[1], u2 = b3[2], u3 = b3[3];
+          gv[7] = u0 * by0 + u1 * by1 + u2 * by2 + u3 * by3;
+          gv[8] = (u1 - u0) * dy0 + (u2 - u1) * dy1 + (u3 - u2) * dy2;
+          const float* z3 = a0 + 7 * wp;
+          gv[9] = z3[0] * by0 + z3[1] * by1 + z3[2] * by2 + z3[3] * by3;
         }
-        const float* qz = a0 + 4 * ws2;  // lateral side 2: offsets +1, +2
-        G[5 * gstride + o] = qz[2] * by2 + qz[3] * by3;
-        const float* qu = a0 + 5 * ws2;  // lateral side 1: offsets -1, 0
-        G[6 * gstride + o] = qu[0] * by0 + qu[1] * by1;
-        const float* b3 = a0 + 6 * ws2;  // 3D spline value
-        float u0 = b3[0], u1 = b3[1], u2 = b3[2], u3 = b3[3];
-        G[7 * gstride + o] = u0 * by0 + u1 * by1 + u2 * by2 + u3 * by3;
-        G[8 * gstride + o] = (u1 - u0) * dy0 + (u2 - u1) * dy1 + (u3 - u2) * dy2;
-        const float* z3 = a0 + 7 * ws2;
-        G[9 * gstride + o] = z3[0] * by0 + z3[1] * by1 + z3[2] * by2 + z3[3] * by3;
+      }
+      if constexpr (MODE == 8) __syncwarp();  // G aliases A (see WarpLayout)
+      if (act) {
+        float* go = G + xr * GS + py;
+#pragma unroll
+        for (int c = 0; c < NG; ++c) go[c * s] = gv[c];
       }
     }
   }
@@ -478,18 +517,17 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     const float bx0 = w[8], bx1 = w[9], bx2 = w[10], bx3 = w[11];
     const float dx0 = w[12], dx1 = w[13], dx2 = w[14];
     const float N = th[2], bg = th[3];
-    const int gstride = wp * s;
     const int s2 = s * s;
     Stride2D ix(lane, s);
     for (int p = lane; p < s2; p += 32, ix.next()) {
       const int px = ix.r, py = ix.c;  // px = jj (X), py = ii (Y)
       int ox = min(max(kxs[px] - 1 - xb, 0), wx - 4);
-      const float* g = G + ox * s + py;
-      float g0 = g[0], g1 = g[s], g2 = g[2 * s], g3 = g[3 * s];
+      const float* g = G + ox * GS + py;  // X node k of map c at g[k * GS + c * s]
+      float g0 = g[0], g1 = g[GS], g2 = g[2 * GS], g3 = g[3 * GS];
       float f = g0 * bx0 + g1 * bx1 + g2 * bx2 + g3 * bx3;
       float dX = (g1 - g0) * dx0 + (g2 - g1) * dx1 + (g3 - g2) * dx2;
-      const float* gy = g + gstride;
-      float dY = gy[0] * bx0 + gy[s] * bx1 + gy[2 * s] * bx2 + gy[3 * s] * bx3;
+      const float* gy = g + s;
+      float dY = gy[0] * bx0 + gy[GS] * bx1 + gy[2 * GS] * bx2 + gy[3 * GS] * bx3;
       float dudt[NV];
       dudt[0] = -N * dX;
       dudt[1] = -N * dY;
@@ -499,33 +537,33 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       if constexpr (MODE != 8) {
 #pragma unroll
         for (int c = 1; c < TR::NA; ++c) {
-          const float* gc = g + (c + 1) * gstride;
-          float dc = gc[0] * bx0 + gc[s] * bx1 + gc[2 * s] * bx2 + gc[3 * s] * bx3;
+          const float* gc = g + (c + 1) * s;
+          float dc = gc[0] * bx0 + gc[GS] * bx1 + gc[2 * GS] * bx2 + gc[3 * GS] * bx3;
           dudt[3 + c] = N * dc;
         }
         if (MODE == 7 && dup45) dudt[5] = dudt[4];
         model = bg + N * f;
       } else {
         // 5D derivatives with the reference's two term corrections
-        const float* gz = g + 2 * gstride;
-        const float* gw = g + 3 * gstride;
-        const float* gu = g + 4 * gstride;
-        const float* gqz = g + 5 * gstride;
-        const float* gqu = g + 6 * gstride;
-        float dZ = gz[0] * bx0 + gz[s] * bx1 + gz[2 * s] * bx2 + gz[3 * s] * bx3 +
-                   (gqz[2 * s] * bx2 + gqz[3 * s] * bx3);
-        float dW = gw[0] * bx0 + gw[s] * bx1 + gw[2 * s] * bx2 + gw[3 * s] * bx3;
-        float dU = gu[0] * bx0 + gu[s] * bx1 + gu[2 * s] * bx2 + gu[3 * s] * bx3 +
-                   (gqu[0] * bx0 + gqu[s] * bx1);
+        const float* gz = g + 2 * s;
+        const float* gw = g + 3 * s;
+        const float* gu = g + 4 * s;
+        const float* gqz = g + 5 * s;
+        const float* gqu = g + 6 * s;
+        float dZ = gz[0] * bx0 + gz[GS] * bx1 + gz[2 * GS] * bx2 + gz[3 * GS] * bx3 +
+                   (gqz[2 * GS] * bx2 + gqz[3 * GS] * bx3);
+        float dW = gw[0] * bx0 + gw[GS] * bx1 + gw[2 * GS] * bx2 + gw[3 * GS] * bx3;
+        float dU = gu[0] * bx0 + gu[GS] * bx1 + gu[2 * GS] * bx2 + gu[3 * GS] * bx3 +
+                   (gqu[0] * bx0 + gqu[GS] * bx1);
         // 3D spline
-        const float* h = g + 7 * gstride;
-        float h0 = h[0], h1 = h[s], h2 = h[2 * s], h3 = h[3 * s];
+        const float* h = g + 7 * s;
+        float h0 = h[0], h1 = h[GS], h2 = h[2 * GS], h3 = h[3 * GS];
         float f3 = h0 * bx0 + h1 * bx1 + h2 * bx2 + h3 * bx3;
         float dX3 = (h1 - h0) * dx0 + (h2 - h1) * dx1 + (h3 - h2) * dx2;
-        const float* hy = g + 8 * gstride;
-        float dY3 = hy[0] * bx0 + hy[s] * bx1 + hy[2 * s] * bx2 + hy[3 * s] * bx3;
-        const float* hz = g + 9 * gstride;
-        float dZ3 = hz[0] * bx0 + hz[s] * bx1 + hz[2 * s] * bx2 + hz[3 * s] * bx3;
+        const float* hy = g + 8 * s;
+        float dY3 = hy[0] * bx0 + hy[GS] * bx1 + hy[2 * GS] * bx2 + hy[3 * GS] * bx3;
+        const float* hz = g + 9 * s;
+        float dZ3 = hz[0] * bx0 + hz[GS] * bx1 + hz[2 * GS] * bx2 + hz[3 * GS] * bx3;
         // mixture (CPUmleFit_LM.cpp:3311-3322)
         const float g2 = th[7], h2m = 1.0f - g2;
         const float m5 = bg + N * f, m3 = bg + N * f3;
@@ -1191,7 +1229,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(128, (MODE == 6 ? BSFIT_MINBLOCKS6 : 1)) fit_kernel(FitArgs a) {
+__global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) fit_kernel(FitArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
   const WarpLayout L = make_layout(MODE, a.s);
@@ -1210,7 +1248,7 @@ __global__ void __launch_bounds__(128, (MODE == 6 ? BSFIT_MINBLOCKS6 : 1)) fit_k
 // fits them, and counts them done. The warp's shared memory is laid out for
 // the largest ROI of the batch.
 template <int MODE>
-__global__ void __launch_bounds__(128, (MODE == 6 ? BSFIT_MINBLOCKS6 : 1)) batch_kernel(const __grid_constant__ BatchArgs a) {
+__global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) batch_kernel(const __grid_constant__ BatchArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
   const int lane = threadIdx.x & 31;

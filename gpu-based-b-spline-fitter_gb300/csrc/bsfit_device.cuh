@@ -70,6 +70,39 @@ __device__ __forceinline__ float axis_weight(float t, int j) {
 }
 
 // ---------------------------------------------------------------------------
+// Four-node contractions in a fixed operation order: the value
+// ((c0 b0 + c1 b1) + c2 b2) + c3 b3 and the difference form
+// ((c1 - c0) d0 + (c2 - c1) d1) + (c3 - c2) d2, each a multiply and a chain of
+// FMAs. The packed forms below evaluate two independent contractions with the
+// same operations per half, so scalar and packed code give identical results.
+
+__device__ __forceinline__ float contract4(float c0, float c1, float c2, float c3, float b0,
+                                           float b1, float b2, float b3) {
+  return fmaf(c3, b3, fmaf(c2, b2, fmaf(c1, b1, c0 * b0)));
+}
+
+__device__ __forceinline__ float dcontract4(float c0, float c1, float c2, float c3, float d0,
+                                            float d1, float d2) {
+  return fmaf(c3 - c2, d2, fmaf(c2 - c1, d1, (c1 - c0) * d0));
+}
+
+// Packed two-lane FP32 (the paired FMA of sm_100 and later): each half is the
+// correctly rounded scalar operation.
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);  // a - b, one rounding
+}
+__device__ __forceinline__ float2 contract4x2(float2 c0, float2 c1, float2 c2, float2 c3,
+                                              float2 b0, float2 b1, float2 b2, float2 b3) {
+  return __ffma2_rn(c3, b3, __ffma2_rn(c2, b2, __ffma2_rn(c1, b1, __fmul2_rn(c0, b0))));
+}
+__device__ __forceinline__ float2 dcontract4x2(float2 c0, float2 c1, float2 c2, float2 c3,
+                                               float2 d0, float2 d1, float2 d2) {
+  return __ffma2_rn(sub2(c3, c2), d2,
+                    __ffma2_rn(sub2(c2, c1), d1, __fmul2_rn(sub2(c1, c0), d0)));
+}
+
+// ---------------------------------------------------------------------------
 // Warp reductions (butterfly: every lane ends with the total).
 
 __device__ __forceinline__ float warp_sum(float v) {

@@ -337,20 +337,44 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       const int64_t sw_ = m.st[3];
       const float* base = m.coeff + (int64_t)(kz - 1) * sz_ + (int64_t)(kw - 1) * sw_;
       Stride2D ix(lane, wy);
+      const float2 BZ0 = bc2(bz0), BZ1 = bc2(bz1), BZ2 = bc2(bz2), BZ3 = bc2(bz3);
+      const float2 DZ0 = bc2(dz0), DZ1 = bc2(dz1), DZ2 = bc2(dz2);
       for (int t = lane; t < nodes; t += 32, ix.next()) {
         const int xr = ix.r, yr = ix.c;
         const float* p = base + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
+        // z contraction of the four w layers: two layers per packed operation
+        // (fit type 7), or one at a time where the packed operands would push
+        // the kernel past its register budget (4Pi, four channels); both
+        // orders of operations are the same.
         float vz[4], dzv[4];
+        if constexpr (MODE == kFit4Pi) {
 #pragma unroll
-        for (int iw = 0; iw < 4; ++iw) {
-          const float* q = p + iw * sw_;
-          float c0 = __ldg(q), c1 = __ldg(q + sz_), c2 = __ldg(q + 2 * sz_), c3 = __ldg(q + 3 * sz_);
-          vz[iw] = c0 * bz0 + c1 * bz1 + c2 * bz2 + c3 * bz3;
-          dzv[iw] = (c1 - c0) * dz0 + (c2 - c1) * dz1 + (c3 - c2) * dz2;
+          for (int iw = 0; iw < 4; ++iw) {
+            const float* q = p + iw * sw_;
+            const float c0 = __ldg(q), c1 = __ldg(q + sz_), c2 = __ldg(q + 2 * sz_), c3 = __ldg(q + 3 * sz_);
+            vz[iw] = contract4(c0, c1, c2, c3, bz0, bz1, bz2, bz3);
+            dzv[iw] = dcontract4(c0, c1, c2, c3, dz0, dz1, dz2);
+          }
+        } else {
+#pragma unroll
+          for (int ip = 0; ip < 2; ++ip) {
+            const float* q0 = p + (2 * ip) * sw_;
+            const float* q1 = q0 + sw_;
+            const float2 c0 = make_float2(__ldg(q0), __ldg(q1));
+            const float2 c1 = make_float2(__ldg(q0 + sz_), __ldg(q1 + sz_));
+            const float2 c2 = make_float2(__ldg(q0 + 2 * sz_), __ldg(q1 + 2 * sz_));
+            const float2 c3 = make_float2(__ldg(q0 + 3 * sz_), __ldg(q1 + 3 * sz_));
+            const float2 v2 = contract4x2(c0, c1, c2, c3, BZ0, BZ1, BZ2, BZ3);
+            const float2 d2 = dcontract4x2(c0, c1, c2, c3, DZ0, DZ1, DZ2);
+            vz[2 * ip] = v2.x;
+            vz[2 * ip + 1] = v2.y;
+            dzv[2 * ip] = d2.x;
+            dzv[2 * ip + 1] = d2.y;
+          }
         }
-        float v = vz[0] * bw[0] + vz[1] * bw[1] + vz[2] * bw[2] + vz[3] * bw[3];
-        float dz = dzv[0] * bw[0] + dzv[1] * bw[1] + dzv[2] * bw[2] + dzv[3] * bw[3];
-        float dwv = (vz[1] - vz[0]) * dw[0] + (vz[2] - vz[1]) * dw[1] + (vz[3] - vz[2]) * dw[2];
+        const float v = contract4(vz[0], vz[1], vz[2], vz[3], bw[0], bw[1], bw[2], bw[3]);
+        const float dz = contract4(dzv[0], dzv[1], dzv[2], dzv[3], bw[0], bw[1], bw[2], bw[3]);
+        const float dwv = dcontract4(vz[0], vz[1], vz[2], vz[3], dw[0], dw[1], dw[2]);
         A[xr * AS + yr] = v;
         A[xr * AS + wp + yr] = dz;
         A[xr * AS + 2 * wp + yr] = dwv;
@@ -398,40 +422,72 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       const float* base = m.coeff + (int64_t)(kz - 1) * sz_ + (int64_t)(kw - 1) * sw_ +
                           (int64_t)(ku - 1) * su_;
       const float* base3 = m.coeff3 + (int64_t)(kz - 1) * sz_;
+      // Packed operands: the z and w weights broadcast to both halves, the
+      // correction weights R of u = 2, 3 side by side.
+      const float2 BZ0 = bc2(bz0), BZ1 = bc2(bz1), BZ2 = bc2(bz2), BZ3 = bc2(bz3);
+      const float2 DZ0 = bc2(dz0), DZ1 = bc2(dz1), DZ2 = bc2(dz2);
+      const float2 BW0 = bc2(bw[0]), BW1 = bc2(bw[1]), BW2 = bc2(bw[2]), BW3 = bc2(bw[3]);
+      const float2 DW0 = bc2(dw[0]), DW1 = bc2(dw[1]), DW2 = bc2(dw[2]);
+      float2 RP[2][2];  // [lvZ-1][lvW-1] = (R(lvU = 1), R(lvU = 2))
+#pragma unroll
+      for (int lz = 0; lz < 2; ++lz)
+#pragma unroll
+        for (int lw = 0; lw < 2; ++lw) RP[lz][lw] = make_float2(R[lz][lw][0], R[lz][lw][1]);
       Stride2D ix(lane, wy);
       for (int t = lane; t < nodes; t += 32, ix.next()) {
         const int xr = ix.r, yr = ix.c;
         const int64_t lat = (int64_t)(xb + xr) * m.st[1] + (yb + yr);
         const float* p = base + lat;
-        float vz[4][4], dzz[4][4];   // [u][w]
-        float qz = 0.0f;             // z-term-27 correction
-        float sq[4][2];              // [u][w in {0,1}]: sum over z in {0,1} of Bz * C
+        // z contraction of the 16 (u, w) columns, u = 2k and 2k + 1 side by
+        // side in one packed operation.
+        float2 vz2[2][4], dzz2[2][4];  // [u pair][w]
+        float2 qz2 = make_float2(0.0f, 0.0f);  // z-term-27 correction, u = 2 | u = 3
+        float2 sq2[2][2];  // [u pair][w in {0,1}]: sum over z in {0,1} of Bz * C
 #pragma unroll
-        for (int iu = 0; iu < 4; ++iu)
+        for (int iw = 0; iw < 4; ++iw)
 #pragma unroll
-          for (int iw = 0; iw < 4; ++iw) {
-            const float* q = p + iu * su_ + iw * sw_;
-            float c0 = __ldg(q), c1 = __ldg(q + sz_), c2 = __ldg(q + 2 * sz_), c3 = __ldg(q + 3 * sz_);
-            vz[iu][iw] = c0 * bz0 + c1 * bz1 + c2 * bz2 + c3 * bz3;
-            dzz[iu][iw] = (c1 - c0) * dz0 + (c2 - c1) * dz1 + (c3 - c2) * dz2;
-            if (iw >= 2 && iu >= 2) {
-              // lvW = iw - 1, lvU = iu - 1; Z nodes 1 - lvZ: local 1 (lvZ 1), 0 (lvZ 2)
-              qz += (c2 - c1) * R[0][iw - 2][iu - 2] + (c1 - c0) * R[1][iw - 2][iu - 2];
+          for (int up = 0; up < 2; ++up) {
+            const float* q0 = p + (2 * up) * su_ + iw * sw_;
+            const float* q1 = q0 + su_;
+            const float2 c0 = make_float2(__ldg(q0), __ldg(q1));
+            const float2 c1 = make_float2(__ldg(q0 + sz_), __ldg(q1 + sz_));
+            const float2 c2 = make_float2(__ldg(q0 + 2 * sz_), __ldg(q1 + 2 * sz_));
+            const float2 c3 = make_float2(__ldg(q0 + 3 * sz_), __ldg(q1 + 3 * sz_));
+            vz2[up][iw] = contract4x2(c0, c1, c2, c3, BZ0, BZ1, BZ2, BZ3);
+            dzz2[up][iw] = dcontract4x2(c0, c1, c2, c3, DZ0, DZ1, DZ2);
+            if (up == 1 && iw >= 2) {
+              // lvW = iw - 1, lvU = u - 1; Z nodes 1 - lvZ: local 1 (lvZ 1), 0 (lvZ 2)
+              qz2 = __fadd2_rn(qz2, __ffma2_rn(sub2(c2, c1), RP[0][iw - 2],
+                                               __fmul2_rn(sub2(c1, c0), RP[1][iw - 2])));
             }
-            if (iw <= 1) sq[iu][iw] = c0 * bz0 + c1 * bz1;
+            if (iw <= 1) sq2[up][iw] = __ffma2_rn(c1, BZ1, __fmul2_rn(c0, BZ0));
           }
         float vw[4], dzw[4], dww[4];
 #pragma unroll
-        for (int iu = 0; iu < 4; ++iu) {
-          vw[iu] = vz[iu][0] * bw[0] + vz[iu][1] * bw[1] + vz[iu][2] * bw[2] + vz[iu][3] * bw[3];
-          dzw[iu] = dzz[iu][0] * bw[0] + dzz[iu][1] * bw[1] + dzz[iu][2] * bw[2] + dzz[iu][3] * bw[3];
-          dww[iu] = (vz[iu][1] - vz[iu][0]) * dw[0] + (vz[iu][2] - vz[iu][1]) * dw[1] +
-                    (vz[iu][3] - vz[iu][2]) * dw[2];
+        for (int up = 0; up < 2; ++up) {
+          const float2 a = contract4x2(vz2[up][0], vz2[up][1], vz2[up][2], vz2[up][3], BW0, BW1, BW2, BW3);
+          const float2 b = contract4x2(dzz2[up][0], dzz2[up][1], dzz2[up][2], dzz2[up][3], BW0, BW1, BW2, BW3);
+          const float2 c = dcontract4x2(vz2[up][0], vz2[up][1], vz2[up][2], vz2[up][3], DW0, DW1, DW2);
+          vw[2 * up] = a.x;
+          vw[2 * up + 1] = a.y;
+          dzw[2 * up] = b.x;
+          dzw[2 * up + 1] = b.y;
+          dww[2 * up] = c.x;
+          dww[2 * up + 1] = c.y;
         }
-        const float v = vw[0] * bu[0] + vw[1] * bu[1] + vw[2] * bu[2] + vw[3] * bu[3];
-        const float dzv = dzw[0] * bu[0] + dzw[1] * bu[1] + dzw[2] * bu[2] + dzw[3] * bu[3];
-        const float dwv = dww[0] * bu[0] + dww[1] * bu[1] + dww[2] * bu[2] + dww[3] * bu[3];
-        const float duv = (vw[1] - vw[0]) * du[0] + (vw[2] - vw[1]) * du[1] + (vw[3] - vw[2]) * du[2];
+        const float v = contract4(vw[0], vw[1], vw[2], vw[3], bu[0], bu[1], bu[2], bu[3]);
+        const float dzv = contract4(dzw[0], dzw[1], dzw[2], dzw[3], bu[0], bu[1], bu[2], bu[3]);
+        const float dwv = contract4(dww[0], dww[1], dww[2], dww[3], bu[0], bu[1], bu[2], bu[3]);
+        const float duv = dcontract4(vw[0], vw[1], vw[2], vw[3], du[0], du[1], du[2]);
+        const float qz = qz2.x + qz2.y;
+        float sq[4][2];
+#pragma unroll
+        for (int iw = 0; iw < 2; ++iw) {
+          sq[0][iw] = sq2[0][iw].x;
+          sq[1][iw] = sq2[0][iw].y;
+          sq[2][iw] = sq2[1][iw].x;
+          sq[3][iw] = sq2[1][iw].y;
+        }
         // u-term-16 correction (CPUsplineLib.cpp:420-421): the term differences
         // the U node at offset 0 instead of +1 with weight
         // By1 Bx1 Bz1 Bw1 dBu2(1); lateral side 1 and z, w at offsets -1 / 0.
@@ -449,8 +505,8 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         o[3 * wp] = duv;
         o[4 * wp] = qz;
         o[5 * wp] = qu;
-        o[6 * wp] = e0 * bz0 + e1 * bz1 + e2 * bz2 + e3 * bz3;
-        o[7 * wp] = (e1 - e0) * dz0 + (e2 - e1) * dz1 + (e3 - e2) * dz2;
+        o[6 * wp] = contract4(e0, e1, e2, e3, bz0, bz1, bz2, bz3);
+        o[7 * wp] = dcontract4(e0, e1, e2, e3, dz0, dz1, dz2);
       }
     }
   }

@@ -83,6 +83,9 @@ struct ModeTraits<6> {
   static constexpr int NA = 2;   // non-lateral maps: value, d/dz
   static constexpr int NG = 3;   // after the Y pass: value, d/dY, d/dz
   static constexpr int NCH = 1;  // image channels per ROI
+  // stage-B maps written over consumed stage-A columns (see WarpLayout): on
+  // where it lets more warps fit per SM
+  static constexpr bool ALIAS = true;
 };
 template <>
 struct ModeTraits<7> {
@@ -91,6 +94,7 @@ struct ModeTraits<7> {
   static constexpr int NA = 3;  // value, d/dz, d/dw
   static constexpr int NG = 4;  // value, d/dY, d/dz, d/dw
   static constexpr int NCH = 1;
+  static constexpr bool ALIAS = false;
 };
 // 4Pi: the 4D evaluation of fit type 7 once per channel.
 template <>
@@ -100,6 +104,7 @@ struct ModeTraits<kFit4Pi> {
   static constexpr int NA = 3;
   static constexpr int NG = 4;
   static constexpr int NCH = k4PiChannels;
+  static constexpr bool ALIAS = false;
 };
 
 template <>
@@ -114,6 +119,7 @@ struct ModeTraits<8> {
   // d/dY, d/dz (3D)
   static constexpr int NG = 10;
   static constexpr int NCH = 1;
+  static constexpr bool ALIAS = true;
 };
 
 // Per-warp shared-memory layout (floats): the ROI's pixels (one plane per
@@ -122,20 +128,33 @@ struct ModeTraits<8> {
 //
 // The stage-A maps (NA per lateral node) and the stage-B maps (NG per X node
 // and pixel row) are both stored by X node ("column"): A column xr holds
-// NA x WP floats, G column xr holds NG x s. For the 5D model, whose maps
-// would otherwise bound the warps per SM by shared memory, the two share one
-// region: stage B reads only A column xr to write G column xr and walks the
+// NA x WP floats, G column xr holds NG x s. For the models whose maps would
+// otherwise bound the warps per SM by shared memory (3D, 5D), the two share
+// one region: stage B reads only A column xr to write G column xr and walks the
 // columns in order, so G is written over A columns already consumed. With G
 // at the start of the region and A at offset a_rel with
 // (xr + 1) * GS <= a_rel + xr * AS for every column, a G column never reaches
 // an A column that is still to be read (the reads and writes of one pass of
 // the warp are separated by __syncwarp). The other models keep the two map
-// sets apart (a_rel = WP * GS) and write G without that synchronisation.
+// sets apart (a_rel = WP * GS) and write G without that synchronisation,
+// which would cost them registers.
+//
+// Bank-conflict-free access: stage B reads A, and stage C reads G, with s
+// lanes per column in each pass of the warp at the same offsets in every
+// column. A's column stride is padded to the next value congruent to s modulo
+// 32, which puts those 32 lanes on 32 consecutive banks. G stores the maps of
+// one (X node, pixel row) item together, GP floats per item with GP odd, so
+// the consecutive items of a pass (stage B writes, stage C reads) sit an odd
+// stride apart: 32 distinct banks.
 struct WarpLayout {
   int s, s2p, wp, na, ng, nch;
   bool alias;
-  __host__ __device__ constexpr int as() const { return na * wp; }  // A column stride
-  __host__ __device__ constexpr int gs() const { return ng * s; }   // G column stride
+  __host__ __device__ static constexpr int bank_pad(int x, int s) {
+    return x + ((s - x) % 32 + 32) % 32;
+  }
+  __host__ __device__ constexpr int as() const { return bank_pad(na * wp, s); }  // A column stride
+  __host__ __device__ constexpr int gp() const { return ng | 1; }               // G item stride
+  __host__ __device__ constexpr int gs() const { return s * gp(); }             // G column stride
   __host__ __device__ constexpr int off_kx() const { return nch * s2p; }
   __host__ __device__ constexpr int off_ky() const { return off_kx() + ((s + 3) & ~3); }
   __host__ __device__ constexpr int off_w() const { return off_ky() + ((s + 3) & ~3); }
@@ -160,7 +179,7 @@ __host__ __device__ constexpr WarpLayout make_layout(int mode, int s) {
   L.na = mode == 6 ? 2 : (mode == 7 || mode == kFit4Pi) ? 3 : 8;
   L.ng = mode == 6 ? 3 : (mode == 7 || mode == kFit4Pi) ? 4 : 10;
   L.nch = mode == kFit4Pi ? k4PiChannels : 1;
-  L.alias = mode == 8;
+  L.alias = mode == 6 || mode == 8;
   return L;
 }
 
@@ -180,10 +199,17 @@ constexpr bool layouts_disjoint() {
         return false;
       for (int c = 0; c < L.wp; ++c)
         if ((c + 1) * L.gs() > L.a_rel() + c * L.as()) return false;
+      if (L.as() < L.na * L.wp || L.gp() < L.ng || (L.as() - s) % 32 != 0 || L.gp() % 2 == 0)
+        return false;
     }
   return true;
 }
 static_assert(layouts_disjoint(), "per-warp shared-memory regions overlap");
+static_assert(make_layout(6, 13).alias == ModeTraits<6>::ALIAS &&
+                  make_layout(7, 13).alias == ModeTraits<7>::ALIAS &&
+                  make_layout(8, 13).alias == ModeTraits<8>::ALIAS &&
+                  make_layout(kFit4Pi, 13).alias == ModeTraits<kFit4Pi>::ALIAS,
+              "layout aliasing and stage-B synchronisation must agree");
 
 int warp_smem_floats(int mode, int s) { return make_layout(mode, s).total(); }
 
@@ -253,9 +279,9 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
   int* kys = reinterpret_cast<int*>(ws + L.off_ky());
   float* w = ws + L.off_w();
   float* A = ws + L.off_a();  // A[xr * AS + map * wp + yr]
-  float* G = ws + L.off_g();  // G[xr * GS + map * s + py]
+  float* G = ws + L.off_g();  // G[(xr * s + py) * GP + map]
   const int wp = L.wp;
-  const int AS = L.as(), GS = L.gs();
+  const int AS = L.as(), GS = L.gs(), GP = L.gp();
   __syncwarp();  // the previous evaluation's readers of kxs / w / G are done
   PHASE_DECL();
 
@@ -513,10 +539,9 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
   __syncwarp();
   PHASE_MARK(1);
 
-  // (B) Y contraction for every (X node, pixel row ii), column by column. For
-  // the 5D model G is written over the A columns already read (the layout's
-  // aliasing rule), so every pass of the warp reads its A values,
-  // synchronises, then writes.
+  // (B) Y contraction for every (X node, pixel row ii), column by column. Where
+  // G is written over the A columns already read (the layout's aliasing rule),
+  // every pass of the warp reads its A values, synchronises, then writes.
   {
     const float by0 = w[0], by1 = w[1], by2 = w[2], by3 = w[3];
     const float dy0 = w[4], dy1 = w[5], dy2 = w[6];
@@ -557,11 +582,11 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
           gv[9] = z3[0] * by0 + z3[1] * by1 + z3[2] * by2 + z3[3] * by3;
         }
       }
-      if constexpr (MODE == 8) __syncwarp();  // G aliases A (see WarpLayout)
+      if constexpr (TR::ALIAS) __syncwarp();  // G aliases A (see WarpLayout)
       if (act) {
-        float* go = G + xr * GS + py;
+        float* go = G + (xr * s + py) * GP;
 #pragma unroll
-        for (int c = 0; c < NG; ++c) go[c * s] = gv[c];
+        for (int c = 0; c < NG; ++c) go[c] = gv[c];
       }
     }
   }
@@ -578,11 +603,11 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     for (int p = lane; p < s2; p += 32, ix.next()) {
       const int px = ix.r, py = ix.c;  // px = jj (X), py = ii (Y)
       int ox = min(max(kxs[px] - 1 - xb, 0), wx - 4);
-      const float* g = G + ox * GS + py;  // X node k of map c at g[k * GS + c * s]
+      const float* g = G + (ox * s + py) * GP;  // X node k of map c at g[k * GS + c]
       float g0 = g[0], g1 = g[GS], g2 = g[2 * GS], g3 = g[3 * GS];
       float f = g0 * bx0 + g1 * bx1 + g2 * bx2 + g3 * bx3;
       float dX = (g1 - g0) * dx0 + (g2 - g1) * dx1 + (g3 - g2) * dx2;
-      const float* gy = g + s;
+      const float* gy = g + 1;
       float dY = gy[0] * bx0 + gy[GS] * bx1 + gy[2 * GS] * bx2 + gy[3 * GS] * bx3;
       float dudt[NV];
       dudt[0] = -N * dX;
@@ -593,7 +618,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       if constexpr (MODE != 8) {
 #pragma unroll
         for (int c = 1; c < TR::NA; ++c) {
-          const float* gc = g + (c + 1) * s;
+          const float* gc = g + (c + 1);
           float dc = gc[0] * bx0 + gc[GS] * bx1 + gc[2 * GS] * bx2 + gc[3 * GS] * bx3;
           dudt[3 + c] = N * dc;
         }
@@ -601,24 +626,24 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         model = bg + N * f;
       } else {
         // 5D derivatives with the reference's two term corrections
-        const float* gz = g + 2 * s;
-        const float* gw = g + 3 * s;
-        const float* gu = g + 4 * s;
-        const float* gqz = g + 5 * s;
-        const float* gqu = g + 6 * s;
+        const float* gz = g + 2;
+        const float* gw = g + 3;
+        const float* gu = g + 4;
+        const float* gqz = g + 5;
+        const float* gqu = g + 6;
         float dZ = gz[0] * bx0 + gz[GS] * bx1 + gz[2 * GS] * bx2 + gz[3 * GS] * bx3 +
                    (gqz[2 * GS] * bx2 + gqz[3 * GS] * bx3);
         float dW = gw[0] * bx0 + gw[GS] * bx1 + gw[2 * GS] * bx2 + gw[3 * GS] * bx3;
         float dU = gu[0] * bx0 + gu[GS] * bx1 + gu[2 * GS] * bx2 + gu[3 * GS] * bx3 +
                    (gqu[0] * bx0 + gqu[GS] * bx1);
         // 3D spline
-        const float* h = g + 7 * s;
+        const float* h = g + 7;
         float h0 = h[0], h1 = h[GS], h2 = h[2 * GS], h3 = h[3 * GS];
         float f3 = h0 * bx0 + h1 * bx1 + h2 * bx2 + h3 * bx3;
         float dX3 = (h1 - h0) * dx0 + (h2 - h1) * dx1 + (h3 - h2) * dx2;
-        const float* hy = g + 8 * s;
+        const float* hy = g + 8;
         float dY3 = hy[0] * bx0 + hy[GS] * bx1 + hy[2 * GS] * bx2 + hy[3 * GS] * bx3;
-        const float* hz = g + 9 * s;
+        const float* hz = g + 9;
         float dZ3 = hz[0] * bx0 + hz[GS] * bx1 + hz[2 * GS] * bx2 + hz[3 * GS] * bx3;
         // mixture (CPUmleFit_LM.cpp:3311-3322)
         const float g2 = th[7], h2m = 1.0f - g2;

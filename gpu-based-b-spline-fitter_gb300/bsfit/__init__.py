@@ -104,6 +104,25 @@ class Model:
                         L.data_ptr(), st.cuda_stream)
         return P, C, L
 
+    def fit_multistart_torch(self, rois, iterations, starts, strict=False, stream=None):
+        """Fused multi-start fit (fit types 7, 8): starts is a sequence of initP
+        vectors; every ROI is fitted from each and the best log-likelihood kept
+        (a later start wins when its LL is higher by >= 1e-4, > 1e-4 if strict).
+        Returns (P (NV+1, N), CRLB (NV, N), LL (N,)) device tensors."""
+        import torch
+        assert rois.is_cuda and rois.dtype == torch.float32 and rois.is_contiguous()
+        st_ = _f32(np.atleast_2d(starts))
+        n, s = rois.shape[0], rois.shape[-1]
+        P = torch.empty((self.nv + 1, n), device=rois.device, dtype=torch.float32)
+        C = torch.empty((self.nv, n), device=rois.device, dtype=torch.float32)
+        L = torch.empty((n,), device=rois.device, dtype=torch.float32)
+        cs = stream if stream is not None else torch.cuda.current_stream(rois.device)
+        check(_native.lib().bsfit_fit_multistart_device(
+            self._h, rois.data_ptr(), s, n, int(iterations), st_.ctypes.data_as(_fp),
+            st_.shape[1], st_.shape[0], int(bool(strict)), P.data_ptr(), C.data_ptr(),
+            L.data_ptr(), cs.cuda_stream), "bsfit_fit_multistart_device")
+        return P, C, L
+
     def trace_torch(self, rois, iterations, flags=0, trace_max=None):
         """Fit with per-iteration decision records; returns (P, CRLB, LL, trace)
         with trace of shape (N, trace_max, 32)."""
@@ -215,6 +234,27 @@ class Model4Pi:
             self._h, rois.data_ptr(), s, n, int(iterations),
             dt.data_ptr() if dt is not None else None, z0.data_ptr(), w0.data_ptr(),
             P.data_ptr(), C.data_ptr(), L.data_ptr(), st.cuda_stream), "bsfit_fit4pi_device")
+        return P, C, L
+
+    def fit_multistart_torch(self, rois, iterations, initZ, initPhi, dT=None, strict=False,
+                             stream=None):
+        """Fused multi-start 4Pi fit: initZ, initPhi of shape (starts, N); the
+        best log-likelihood over the starts is kept per ROI (the demo's rule)."""
+        import torch
+        n, s = rois.shape[1], rois.shape[-1]
+        z0 = initZ.contiguous()
+        w0 = initPhi.contiguous()
+        k = z0.shape[0] if z0.dim() == 2 else 1
+        dt = dT.contiguous() if dT is not None else None
+        P = torch.empty((7, n), device=rois.device, dtype=torch.float32)
+        C = torch.empty((6, n), device=rois.device, dtype=torch.float32)
+        L = torch.empty((n,), device=rois.device, dtype=torch.float32)
+        cs = stream if stream is not None else torch.cuda.current_stream(rois.device)
+        check(_native.lib().bsfit_fit4pi_multistart_device(
+            self._h, rois.data_ptr(), s, n, int(iterations),
+            dt.data_ptr() if dt is not None else None, z0.data_ptr(), w0.data_ptr(), k,
+            int(bool(strict)), P.data_ptr(), C.data_ptr(), L.data_ptr(), cs.cuda_stream),
+            "bsfit_fit4pi_multistart_device")
         return P, C, L
 
     def eval_torch(self, rois, theta, dT=None, fisher=False, stream=None):

@@ -544,4 +544,71 @@ int bsfit_GPUmleFit_LM_4Pi_bspline(const float* imstack, int64_t roi_size, int64
   return cuda_status(e);
 }
 
+// ---------------------------------------------------------------------------
+// Multi-start, fused: every ROI fitted from each start in one launch, the ROI
+// staged once, the best log-likelihood kept (the callers' loop at
+// MultiD_fitter/simplefitter_cspline.m:463-490, demo_orientation/store/fitb5n3.m:15-46,
+// demo_4pi/bspline_based_4piloc_v4.m:193-215).
+
+int bsfit_fit_multistart_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                                int64_t nfits, int32_t iterations, const float* init_p_starts,
+                                int32_t start_len, int32_t n_starts, int32_t strict, float* d_P,
+                                float* d_CRLB, float* d_LL, void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  const int ft = model->dev.fittype;
+  if (ft != 7 && ft != 8) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0 || n_starts < 1 || n_starts > bsfit::kMaxStarts) return BSFIT_E_INVALID;
+  if (!init_p_starts || start_len < (ft == 7 ? 2 : 4) || start_len > 64) return BSFIT_E_INIT_P;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  a.out_n = nfits;
+  a.n_starts = n_starts;
+  a.strict = strict ? 1 : 0;
+  for (int k = 0; k < n_starts; ++k)
+    for (int i = 0; i < 4; ++i)
+      a.starts[k][i] = i < start_len ? init_p_starts[(int64_t)k * start_len + i] : 0.0f;
+  return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
+}
+
+int bsfit_fit4pi_multistart_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                                   int64_t nfits, int32_t iterations, const float* d_dT,
+                                   const float* d_initZ, const float* d_initPhi, int32_t n_starts,
+                                   int32_t strict, float* d_P, float* d_CRLB, float* d_LL,
+                                   void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  if (model->dev.fittype != bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0 || n_starts < 1 || n_starts > bsfit::kMaxStarts) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_initZ || !d_initPhi || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  a.out_n = nfits;
+  a.dT = d_dT;
+  a.z0 = d_initZ;
+  a.w0 = d_initPhi;
+  a.n_starts = n_starts;
+  a.strict = strict ? 1 : 0;
+  return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
+}
+
 }  // extern "C"

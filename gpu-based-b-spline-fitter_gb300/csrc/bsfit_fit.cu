@@ -931,12 +931,22 @@ __device__ __forceinline__ void initial_guess(const float* data, int s, int lane
   g[3] = (mn > 0.01f) ? mn : 0.01f;
 }
 
+// Result of one fit, distributed like the LM state: lane l < NV holds
+// parameter l and its variance; the log-likelihood and the iteration count are
+// on every lane.
+struct RoiResult {
+  float par, crlb, ll;
+  int kk;
+};
+
+// Fit of the ROI staged in ws (load_roi) from start `start` (0 unless
+// multi-start).
 template <int MODE>
-__device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int lane, int64_t roi) {
+__device__ RoiResult fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int lane, int64_t roi,
+                             int start) {
   using TR = ModeTraits<MODE>;
   constexpr int NV = TR::NV;
   const int s = L.s;
-  load_roi<MODE>(a, L, ws, lane, roi);
 
   PHASE_DECL();
   // Initial guesses (CPUgaussLib.cpp:172-225, CPUmleFit_LM.cpp:2477-2482),
@@ -966,16 +976,19 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
     if (MODE == 6) {
       if (lane == 4) v = (float)a.m.n[2] / 2.0f;
     } else if (MODE == 7) {
-      const bool use = a.m.init_p_len >= 2 && a.m.init_p[0] != 0.0f;
-      if (lane == 4) v = use ? a.m.init_p[0] : (float)a.m.n[2] / 2.0f;
-      if (lane == 5) v = use ? a.m.init_p[1] : (float)a.m.n[3] / 2.0f;
+      const float* ip = (a.n_starts > 0) ? a.starts[start] : a.m.init_p;
+      const bool use = (a.n_starts > 0 || a.m.init_p_len >= 2) && ip[0] != 0.0f;
+      if (lane == 4) v = use ? ip[0] : (float)a.m.n[2] / 2.0f;
+      if (lane == 5) v = use ? ip[1] : (float)a.m.n[3] / 2.0f;
     } else if (MODE == 8) {
       // (z, w, u, g2) from initP, shared by all ROIs (CPUmleFit_LM.cpp:3246-3256)
-      if (lane >= 4 && lane < 8) v = a.m.init_p[lane - 4];
+      const float* ip = (a.n_starts > 0) ? a.starts[start] : a.m.init_p;
+      if (lane >= 4 && lane < 8) v = ip[lane - 4];
     } else {
-      // 4Pi: per-ROI initial z and phase
-      if (lane == 4) v = a.z0[roi];
-      if (lane == 5) v = wrap_phase(a.w0[roi], a.m.n[3]);
+      // 4Pi: per-ROI initial z and phase, one array per start
+      const int64_t i0 = (int64_t)start * a.nfits + roi;
+      if (lane == 4) v = a.z0[i0];
+      if (lane == 5) v = wrap_phase(a.w0[i0], a.m.n[3]);
     }
     par = v;
   }
@@ -1024,7 +1037,7 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
       need_eval = true;
       continue;
     }
-    float* rec = (a.trace && kk < a.trace_max && lane == 0)
+    float* rec = (a.trace && start == 0 && kk < a.trace_max && lane == 0)
                      ? a.trace + (roi * (int64_t)a.trace_max + kk) * TRACE_REC
                      : nullptr;
     // |(newErr - oldErr) / newErr| < 1e-6 (CPUmleFit_LM.cpp:2565)
@@ -1294,22 +1307,55 @@ __device__ void fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int la
       if (lane == c && dk[c] == 0.0f) crlb = __int_as_float(0x7f800000);
   }
   PHASE_MARK(7);
+  return RoiResult{par, crlb, ll.hi + ll.lo, kk};
+}
+
+template <int MODE>
+__device__ __forceinline__ void store_result(const FitArgs& a, int lane, int64_t roi,
+                                             const RoiResult& r) {
+  constexpr int NV = ModeTraits<MODE>::NV;
   float thv[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) thv[k] = bcast(par, k);
+  for (int k = 0; k < NV; ++k) thv[k] = bcast(r.par, k);
   if (lane == 0) {
     const int64_t n = a.out_n;
     const int64_t o = a.out_offset + roi;
 #pragma unroll
     for (int i = 0; i < NV; ++i) a.P[i * n + o] = thv[i];
-    a.P[NV * n + o] = (float)kk;
-    a.LL[o] = ll.hi + ll.lo;
+    a.P[NV * n + o] = (float)r.kk;
+    a.LL[o] = r.ll;
   }
-  if (lane < NV) a.CRLB[lane * a.out_n + a.out_offset + roi] = crlb;
+  if (lane < NV) a.CRLB[lane * a.out_n + a.out_offset + roi] = r.crlb;
   __syncwarp();
 }
 
-template <int MODE>
+// Fit one ROI from every start and store the kept result. The ROI is staged
+// once; a later start replaces the kept result when its log-likelihood is
+// higher by more than 1e-4 (strict) or by at least 1e-4, the rule of the
+// reference's multi-start callers (MultiD_fitter/simplefitter_cspline.m:480-490,
+// demo_orientation/store/fitb5n3.m:36-45, demo_4pi/bspline_based_4piloc_v4.m:201-214).
+// MULTI selects the multi-start kernels; the single-start ones carry no start
+// loop (it would cost them registers).
+template <int MODE, bool MULTI>
+__device__ __forceinline__ void fit_and_store(const FitArgs& a, const WarpLayout& L, float* ws,
+                                              int lane, int64_t roi) {
+  load_roi<MODE>(a, L, ws, lane, roi);
+  if constexpr (MULTI) {
+    // one call site for all starts (a second inlined copy of the fit would
+    // double the kernel's instruction footprint)
+    RoiResult best{0.0f, 0.0f, 0.0f, 0};
+    for (int k = 0; k < a.n_starts; ++k) {
+      const RoiResult r = fit_roi<MODE>(a, L, ws, lane, roi, k);
+      const float d = r.ll - best.ll;
+      if (k == 0 || (a.strict ? (d > 1e-4f) : (d >= 1e-4f))) best = r;
+    }
+    store_result<MODE>(a, lane, roi, best);
+  } else {
+    store_result<MODE>(a, lane, roi, fit_roi<MODE>(a, L, ws, lane, roi, 0));
+  }
+}
+
+template <int MODE, bool MULTI>
 __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) fit_kernel(FitArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
@@ -1320,7 +1366,7 @@ __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) fit_kernel(FitArgs
   float* ws = smem + wib * L.total();
   const int64_t total_warps = (int64_t)gridDim.x * wpb;
   for (int64_t roi = (int64_t)blockIdx.x * wpb + wib; roi < a.nfits; roi += total_warps)
-    fit_roi<MODE>(a, L, ws, lane, roi);
+    fit_and_store<MODE, MULTI>(a, L, ws, lane, roi);
 }
 
 // Persistent batched fit: every warp claims ROIs one at a time from the
@@ -1359,7 +1405,12 @@ __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) batch_kernel(const
     fa.trace = nullptr;
     fa.trace_max = 0;
     fa.flags = a.flags;
-    fit_roi<MODE>(fa, make_layout(MODE, g.s), ws, lane, (int64_t)i);
+    fa.dT = nullptr;
+    fa.z0 = nullptr;
+    fa.w0 = nullptr;
+    fa.n_starts = 0;
+    fa.strict = 0;
+    fit_and_store<MODE, false>(fa, make_layout(MODE, g.s), ws, lane, (int64_t)i);
     if (lane == 0) atomicAdd(&a.done[g.slot], 1ull);
   }
 }
@@ -1518,10 +1569,11 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
   const int mode = a.m.fittype;
   const int per_warp = warp_smem_floats(mode, a.s) * 4;
   void (*kern)(FitArgs) = nullptr;
-  if (mode == 6) kern = fit_kernel<6>;
-  else if (mode == 7) kern = fit_kernel<7>;
-  else if (mode == 8) kern = fit_kernel<8>;
-  else if (mode == kFit4Pi) kern = fit_kernel<kFit4Pi>;
+  const bool multi = a.n_starts > 1;
+  if (mode == 6) kern = fit_kernel<6, false>;
+  else if (mode == 7) kern = multi ? fit_kernel<7, true> : fit_kernel<7, false>;
+  else if (mode == 8) kern = multi ? fit_kernel<8, true> : fit_kernel<8, false>;
+  else if (mode == kFit4Pi) kern = multi ? fit_kernel<kFit4Pi, true> : fit_kernel<kFit4Pi, false>;
   else return cudaErrorInvalidValue;
   // Warps per block: the choice among 4, 2, 1 that keeps the most warps
   // resident per SM (shared memory per warp grows with s and the model).

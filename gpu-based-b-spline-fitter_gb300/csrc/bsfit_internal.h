@@ -43,11 +43,20 @@ struct FitArgs {
   int trace_max;
   int flags;
   // 4Pi only: per-ROI channel offsets dT [nfits][4][6], initial z and phase
-  // [nfits]; rois holds [4][nfits][s][s].
+  // [n_starts or 1][nfits]; rois holds [4][nfits][s][s].
   const float* dT;
   const float* z0;
   const float* w0;
+  // Multi-start: n_starts > 1 fits every ROI from each start and keeps the
+  // best log-likelihood (a later start replaces the kept result when its LL is
+  // higher by more than 1e-4, or by at least 1e-4 unless strict). Fit types 7
+  // and 8 take the starts' initP vectors from starts[]; 4Pi from z0 / w0.
+  int n_starts;
+  int strict;
+  float starts[8][4];
 };
+
+constexpr int kMaxStarts = 8;
 
 constexpr int TRACE_REC = 32;
 constexpr int FLAG_NO_REFINE = 1;  // skip the refinement step of the LM solve

@@ -301,6 +301,31 @@ int bsfit_eval4pi_device(bsfit_model model, const float* d_rois, int64_t roi_siz
                          const float* d_dT, const float* d_theta, int32_t fisher, float* d_out,
                          void* stream);
 
+/*
+ * Multi-start, fused into one launch (no reference counterpart as one call:
+ * the reference's callers loop over starts, re-uploading and refitting the
+ * whole stack each time, MultiD_fitter/simplefitter_cspline.m:463-490,
+ * demo_orientation/store/fitb5n3.m:15-46, demo_4pi/bspline_based_4piloc_v4.m:193-215).
+ * Each ROI is staged once and fitted from every start; the result of a later
+ * start replaces the kept one when its log-likelihood is higher by at least
+ * 1e-4 (strict != 0: by more than 1e-4), the callers' rule, so the outputs
+ * equal those loops over single-start calls.
+ * Fit types 7 and 8: init_p_starts is a host array of n_starts x start_len
+ * initP vectors (start_len >= 2 for 7, >= 4 for 8), n_starts <= 8. Fit type 6
+ * has no initP and returns BSFIT_E_UNSUPPORTED_FITTYPE.
+ * 4Pi: d_initZ and d_initPhi hold n_starts x nfits values (start-major).
+ */
+#define BSFIT_MAX_STARTS 8
+int bsfit_fit_multistart_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                                int64_t nfits, int32_t iterations, const float* init_p_starts,
+                                int32_t start_len, int32_t n_starts, int32_t strict, float* d_P,
+                                float* d_CRLB, float* d_LL, void* stream);
+int bsfit_fit4pi_multistart_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                                   int64_t nfits, int32_t iterations, const float* d_dT,
+                                   const float* d_initZ, const float* d_initPhi, int32_t n_starts,
+                                   int32_t strict, float* d_P, float* d_CRLB, float* d_LL,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -414,6 +414,27 @@ def bench_gpu(args):
             b4.record(stream)
         stream.synchronize()
         fits_4pi = w4.n_fits / (a4.elapsed_time(b4) / 2 * 1e-3)
+    # Coefficient builder (bsarray, degree 3) on the 5D grid: GPU kernel
+    # against the numpy restatement on the host.
+    prefilter_fig = None
+    if not args.no_prefilter:
+        from bsfit import prefilter as PF
+        grid = (9, 18, 41, 34, 34)  # (U, W, Z, X, Y) of the 5D figure's model
+        smp = np.random.default_rng(3).random(grid)
+        xs = torch.from_numpy(smp).to(dev)
+        with torch.cuda.stream(stream):
+            bsfit.bsarray_coeffs_torch(xs, stream=stream)
+            ap, bp = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ap.record(stream)
+            for _ in range(3):
+                bsfit.bsarray_coeffs_torch(xs, stream=stream)
+            bp.record(stream)
+        stream.synchronize()
+        t0 = time.perf_counter()
+        PF.bsarray_coeffs(smp)
+        cpu_s = time.perf_counter() - t0
+        prefilter_fig = {"grid": "x".join(str(g) for g in reversed(grid)) + " (Y, X, Z, W, U) float64",
+                         "gpu_ms": ap.elapsed_time(bp) / 3, "cpu_numpy_ms": cpu_s * 1e3}
     serving = None if args.no_serve else bench_serving(args, dev)
     if rank != 0:
         return 0
@@ -457,6 +478,7 @@ def bench_gpu(args):
                        "5d_workload": f"{args.rois_5d} ROIs 17x17, fit type 8, 60 iterations",
                        "4pi_13px": fits_4pi,
                        "4pi_workload": f"{args.rois_4pi} ROIs of 4 channels 13x13, 100 iterations"},
+        "prefilter": prefilter_fig,
         "serving": serving,
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
@@ -481,6 +503,7 @@ def main():
     ap.add_argument("--no-5d", action="store_true")
     ap.add_argument("--rois-4pi", type=int, default=100000, help="ROIs of the 4Pi figure")
     ap.add_argument("--no-4pi", action="store_true")
+    ap.add_argument("--no-prefilter", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-frames", type=int, default=80)
     args = ap.parse_args()

@@ -419,6 +419,38 @@ class Server:
             pass
 
 
+def bsarray_coeffs(samples):
+    """Cubic B-spline coefficients of a sampled stack on the GPU (the
+    reference's bsarray, degree 3): samples in C order with the reference's
+    fastest axis last, shape (..., Z, X, Y); returns float32 coefficients two
+    larger along every axis, the fitter's coefficient input."""
+    x = np.ascontiguousarray(samples, dtype=np.float64)
+    out = np.empty(tuple(d + 2 for d in x.shape), np.float32)
+    check(_native.lib().bsfit_bsarray_coeffs(
+        x.ctypes.data_as(np.ctypeslib.ctypes.POINTER(np.ctypeslib.ctypes.c_double)), x.ndim,
+        _dims(x), out.ctypes.data_as(_fp)), "bsfit_bsarray_coeffs")
+    return out
+
+
+def bsarray_coeffs_torch(samples, out64=False, stream=None):
+    """Device form: samples a CUDA float64 tensor (C order, reference's fastest
+    axis last); returns the float32 coefficients (and the float64 ones with
+    out64) as CUDA tensors."""
+    import torch
+    x = samples.contiguous()
+    assert x.is_cuda and x.dtype == torch.float64
+    shape = tuple(d + 2 for d in x.shape)
+    work = torch.empty_like(x)
+    c32 = torch.empty(shape, device=x.device, dtype=torch.float32)
+    c64 = torch.empty(shape, device=x.device, dtype=torch.float64) if out64 else None
+    dims = (np.ctypeslib.ctypes.c_int64 * x.dim())(*reversed(x.shape))
+    cs = stream if stream is not None else torch.cuda.current_stream(x.device)
+    check(_native.lib().bsfit_bsarray_coeffs_device(
+        x.data_ptr(), x.dim(), dims, work.data_ptr(), c32.data_ptr(),
+        c64.data_ptr() if c64 is not None else None, cs.cuda_stream), "bsfit_bsarray_coeffs_device")
+    return (c32, c64) if out64 else c32
+
+
 def measure_fp32_peak():
     """Measured FP32 FMA throughput of the current device, TFLOP/s."""
     v = np.ctypeslib.ctypes.c_double()

@@ -71,6 +71,11 @@ SIGNATURES = {
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "bsfit_bsarray_coeffs_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32, _i64p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p]),
+    "bsfit_bsarray_coeffs": (ctypes.c_int, [
+        ctypes.POINTER(ctypes.c_double), ctypes.c_int32, _i64p, _fp]),
     "bsfit_eval4pi_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
         ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),

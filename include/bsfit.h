@@ -326,6 +326,23 @@ int bsfit_fit4pi_multistart_device(bsfit_model model, const float* d_rois, int64
                                    int32_t strict, float* d_P, float* d_CRLB, float* d_LL,
                                    void* stream);
 
+/*
+ * Cubic B-spline coefficients of a sampled PSF stack on the device: the
+ * reference's coefficient builder bsarray for degree 3 without smoothing (the
+ * mirror-boundary cubic prefilter along every axis, then a one-sample mirror
+ * pad; MultiD_bspline/bsarray/directFilter.m:200-298, symExpFilt.m:27-44,
+ * getBSplineFiltCoeffs.m:45-50), in double as the MATLAB builder computes.
+ * d_samples: double, ndim <= 5 axes with dims[0] fastest (MATLAB order);
+ * d_work: double scratch of the samples' size; outputs: d_coeff (float, the
+ * fitter's coefficient input) and/or d_coeff64 (double), prod(dims[i] + 2)
+ * elements each. Either output may be NULL, not both.
+ */
+int bsfit_bsarray_coeffs_device(const double* d_samples, int32_t ndim, const int64_t* dims,
+                                double* d_work, float* d_coeff, double* d_coeff64,
+                                void* stream);
+/* The same with host buffers, synchronous: float coefficients out. */
+int bsfit_bsarray_coeffs(const double* samples, int32_t ndim, const int64_t* dims, float* coeff);
+
 #ifdef __cplusplus
 }
 #endif

@@ -451,6 +451,54 @@ def bsarray_coeffs_torch(samples, out64=False, stream=None):
     return (c32, c64) if out64 else c32
 
 
+def peak_kernel(mode, sigma):
+    """The reference's peak-finding filter kernel (0: Gaussian, 1: difference of
+    Gaussians) as a (k, k) float32 array h[u, v] (u the row offset)."""
+    buf = np.zeros(31 * 31, np.float32)
+    k = np.ctypeslib.ctypes.c_int32()
+    check(_native.lib().bsfit_peak_kernel(int(mode), float(sigma), buf.ctypes.data_as(_fp),
+                                          np.ctypeslib.ctypes.byref(k)), "bsfit_peak_kernel")
+    return buf[:k.value * k.value].reshape(k.value, k.value).T.copy()
+
+
+def find_rois_torch(frames, offset, conversion, kernel, dog, cutoff, roi_size, mirror=False,
+                    capacity=None, filtered=False, stream=None):
+    """Frame -> ROI front end on the GPU. frames: CUDA float32 (F, W, H) (the
+    C-order view of MATLAB [H, W, F]); kernel: (k, k) float array h[u, v];
+    dog: subtract the first column's minimum before filtering. Returns
+    (rois (N, s, s), coords (N, 3) = x, y, frame 1-based[, filtered (F, W, H)])
+    as CUDA tensors, N the number found (all of them)."""
+    import torch
+    assert frames.is_cuda and frames.dtype == torch.float32
+    fr = frames.contiguous()
+    F, W, H = fr.shape
+    h = np.ascontiguousarray(np.asarray(kernel, np.float32).T)  # [u + k v]
+    fe = _native.Frontend(float(offset), float(conversion), h.ctypes.data_as(_fp), h.shape[0],
+                          int(bool(dog)), float(cutoff), int(roi_size), int(bool(mirror)))
+    lib = _native.lib()
+    nb = lib.bsfit_find_rois_scratch_bytes(F, H, W)
+    scratch = torch.empty((max(nb, 256),), dtype=torch.uint8, device=fr.device)
+    filt = torch.empty_like(fr) if filtered else None
+    cs = stream if stream is not None else torch.cuda.current_stream(fr.device)
+    s = int(roi_size)
+    cap = int(capacity) if capacity is not None else max(1, F * W * H // 100)
+    for _ in range(2):
+        rois = torch.empty((cap, s, s), dtype=torch.float32, device=fr.device)
+        coords = torch.empty((3, cap), dtype=torch.float32, device=fr.device)
+        n = np.ctypeslib.ctypes.c_int64()
+        check(lib.bsfit_find_rois_device(fr.data_ptr(), F, H, W, np.ctypeslib.ctypes.byref(fe),
+                                         rois.data_ptr(), coords.data_ptr(), cap,
+                                         np.ctypeslib.ctypes.byref(n),
+                                         filt.data_ptr() if filt is not None else None,
+                                         scratch.data_ptr(), nb, cs.cuda_stream), "bsfit_find_rois_device")
+        if n.value <= cap or capacity is not None:
+            break
+        cap = n.value
+    k = min(n.value, cap)
+    out = (rois[:k], coords[:, :k].T.contiguous())
+    return out + (filt,) if filtered else out
+
+
 def measure_fp32_peak():
     """Measured FP32 FMA throughput of the current device, TFLOP/s."""
     v = np.ctypeslib.ctypes.c_double()

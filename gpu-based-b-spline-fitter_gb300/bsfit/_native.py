@@ -76,6 +76,13 @@ SIGNATURES = {
         ctypes.c_void_p]),
     "bsfit_bsarray_coeffs": (ctypes.c_int, [
         ctypes.POINTER(ctypes.c_double), ctypes.c_int32, _i64p, _fp]),
+    "bsfit_peak_kernel": (ctypes.c_int, [ctypes.c_int32, ctypes.c_double, _fp,
+                                         ctypes.POINTER(ctypes.c_int32)]),
+    "bsfit_find_rois_scratch_bytes": (ctypes.c_int64, [ctypes.c_int64] * 3),
+    "bsfit_find_rois_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64),
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "bsfit_eval4pi_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
         ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
@@ -115,6 +122,14 @@ class Segment(ctypes.Structure):
                 ("roi_size", ctypes.c_int64), ("nfits", ctypes.c_int64),
                 ("iterations", ctypes.c_int32), ("d_P", ctypes.c_void_p),
                 ("d_CRLB", ctypes.c_void_p), ("d_LL", ctypes.c_void_p)]
+
+
+class Frontend(ctypes.Structure):
+    """bsfit_frontend (include/bsfit.h)."""
+    _fields_ = [("offset", ctypes.c_float), ("conversion", ctypes.c_float),
+                ("kernel", ctypes.POINTER(ctypes.c_float)), ("ksize", ctypes.c_int32),
+                ("subtract_first_column_min", ctypes.c_int32), ("cutoff", ctypes.c_double),
+                ("roi_size", ctypes.c_int32), ("mirror", ctypes.c_int32)]
 
 
 class HostSegment(ctypes.Structure):

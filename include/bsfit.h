@@ -343,6 +343,46 @@ int bsfit_bsarray_coeffs_device(const double* d_samples, int32_t ndim, const int
 /* The same with host buffers, synchronous: float coefficients out. */
 int bsfit_bsarray_coeffs(const double* samples, int32_t ndim, const int64_t* dims, float* coeff);
 
+/*
+ * Frame -> ROI front end (the step before the fit in the reference's
+ * acquisition loop, MultiD_fitter/simplefitter_cspline.m:197-319, with the peak
+ * finder MultiD_fitter/shared/maximumfind2.c): photon conversion, filtering,
+ * strict 3x3 non-maximum suppression, the cutoff and border filter, and the ROI
+ * cut-out, on a stack of frames in device memory.
+ */
+typedef struct bsfit_frontend {
+  float offset;      /* imphot = (frame - offset) * conversion (single precision) */
+  float conversion;
+  const float* kernel;  /* host, ksize x ksize filter kernel h(u, v) at kernel[u + ksize v] */
+  int32_t ksize;        /* 1 .. 31 */
+  int32_t subtract_first_column_min;  /* 1: filter imphot - min(imphot(:, 1)) (difference of Gaussians) */
+  double cutoff;        /* keep maxima whose filtered value exceeds it */
+  int32_t roi_size;     /* odd, <= 51 */
+  int32_t mirror;       /* cut ROIs with x reversed */
+} bsfit_frontend;
+
+/* The reference's peak-finding kernels (simplefitter_cspline.m:197-211): mode 0
+ * fspecial('gaussian', max(3, ceil(3 sigma + 1)), sigma); mode 1 the difference
+ * of Gaussians of size max(ceil(6 sigma + 1), 3) with widths sigma and
+ * max(1, 2.5 sigma). kernel holds at least 31 x 31 floats. Host only. */
+int bsfit_peak_kernel(int32_t mode, double sigma, float* kernel, int32_t* ksize);
+
+/* Scratch bytes for bsfit_find_rois_device. */
+int64_t bsfit_find_rois_scratch_bytes(int64_t nframes, int64_t height, int64_t width);
+
+/* d_frames: float [nframes][width][height] (MATLAB [height, width, nframes]),
+ * nframes <= 65535. Writes, in the reference's order (frames, then columns,
+ * then rows), up to `capacity` ROIs to d_rois ([capacity][s][s], the fitter's
+ * layout) and their coordinates to d_coords (column-major [capacity x 3]: x, y
+ * 1-based, frame number from 1). *n_found is the number of ROIs found, which
+ * may exceed capacity (only the first `capacity` are written). d_filtered, if
+ * not NULL, receives the filtered frames. Synchronises `stream` before
+ * returning (for n_found). */
+int bsfit_find_rois_device(const float* d_frames, int64_t nframes, int64_t height, int64_t width,
+                           const bsfit_frontend* fe, float* d_rois, float* d_coords,
+                           int64_t capacity, int64_t* n_found, float* d_filtered, void* d_scratch,
+                           int64_t scratch_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -3,6 +3,7 @@
 # (read-only) into oracle/_ref/, as the checker for the oracle restatement:
 #   oracle/_ref/libref_f32.so  FP32, as shipped
 #   oracle/_ref/libref_f64.so  the same sources with float promoted to double
+#   oracle/_ref/libref_maxfind.so  the peak finder MultiD_fitter/shared/maximumfind2.c
 # Only the three fitter sources are compiled (not erf.cpp, which the reference's
 # own project does not build, nor the mex driver, which needs MATLAB).
 # -fno-stack-protector: the 8-parameter solver kernel_luEvaluate5D declares
@@ -37,4 +38,14 @@ for variant in f32 f64; do
   "$CXX" -shared -Wl,--no-undefined -o "$OUT/libref_$variant.so" "${objs[@]}" -lm
   rm -f "${objs[@]}"
 done
-echo "built $OUT/libref_f32.so $OUT/libref_f64.so"
+# The reference's peak finder (non-maximum suppression of the frame front end),
+# compiled as C with a mex.h stand-in; only its NMS function is called.
+PEAK="$REF/MultiD_fitter/shared/maximumfind2.c"
+if [ -f "$PEAK" ]; then
+  CC="${CC:-gcc}"
+  "$CC" -O2 -fPIC -w -I "$HERE/ref_shim_mex" -c "$PEAK" -o "$OUT/maximumfind2.o"
+  "$CC" -O2 -fPIC -w -I "$HERE/ref_shim_mex" -c "$HERE/ref_shim_mex/mex_stubs.c" -o "$OUT/mex_stubs.o"
+  "$CC" -shared -Wl,--no-undefined -o "$OUT/libref_maxfind.so" "$OUT/maximumfind2.o" "$OUT/mex_stubs.o"
+  rm -f "$OUT/maximumfind2.o" "$OUT/mex_stubs.o"
+fi
+echo "built $OUT/libref_f32.so $OUT/libref_f64.so $OUT/libref_maxfind.so"

@@ -283,6 +283,71 @@ def bench_serving(args, dev, seed=11):
             "max_inflight": 4, "arena_bytes": 4 << 30}
 
 
+def synthetic_movie(F=64, H=512, W=512, per_frame=150, seed=31, offset=100.0, conversion=0.5):
+    """ADU frames (F, W, H) = MATLAB [H, W, F]: Poisson background 12 e- and
+    astigmatic emitters (1000-5000 e-, z uniform +-600 nm) at random positions."""
+    from bsfit import workloads as W_
+    rng = np.random.default_rng(seed)
+    frames = np.empty((F, W, H), np.float32)
+    for f in range(F):
+        lam = np.full((W, H), 12.0)
+        xs = rng.uniform(8, W - 8, per_frame)
+        ys = rng.uniform(8, H - 8, per_frame)
+        zs = rng.uniform(-600, 600, per_frame)
+        ns = np.exp(rng.uniform(np.log(1000), np.log(5000), per_frame))
+        sx, sy = W_.astig_sigmas(zs, 1.3)
+        for x, y, a, b, n in zip(xs, ys, sx, sy, ns):
+            x0, y0 = int(x) - 7, int(y) - 7
+            gx = W_._int_gauss(np.array([x - x0]), np.array([a]), 15)[0]
+            gy = W_._int_gauss(np.array([y - y0]), np.array([b]), 15)[0]
+            lam[x0:x0 + 15, y0:y0 + 15] += n * gx[:, None] * gy[None, :]
+        frames[f] = (rng.poisson(lam) / conversion + offset).astype(np.float32)
+    return frames
+
+
+def bench_frontend(dev, stream):
+    """Frame -> ROI front end (difference-of-Gaussians filter, sigma 1, 13 px
+    ROIs) on a 64-frame 512 x 512 movie, alone and followed by the 3D fit of the
+    ROIs it finds (frames resident on the device); the numpy restatement of the
+    front end on two frames for comparison."""
+    import torch
+    import bsfit
+    from bsfit import workloads as W
+    frames = synthetic_movie()
+    fr = torch.from_numpy(frames).to(dev)
+    h = bsfit.peak_kernel(1, 1.0)
+    model = bsfit.Model(6, W.coeff3d())
+    kw = dict(dog=True, cutoff=8.0, roi_size=13, stream=stream)
+    with torch.cuda.stream(stream):
+        rois, coords = bsfit.find_rois_torch(fr, 100.0, 0.5, h, **kw)
+        model.fit_torch(rois.contiguous(), 30, stream=stream)
+    stream.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            rois, coords = bsfit.find_rois_torch(fr, 100.0, 0.5, h, capacity=len(coords), **kw)
+        stream.synchronize()
+    fe_s = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            rois, coords = bsfit.find_rois_torch(fr, 100.0, 0.5, h, capacity=len(coords), **kw)
+            model.fit_torch(rois.contiguous(), 30, stream=stream)
+        stream.synchronize()
+    both_s = (time.perf_counter() - t0) / reps
+    from oracle import frontend as FE  # CPU comparison leg only
+    t0 = time.perf_counter()
+    FE.find_rois(frames[:2], 100.0, 0.5, FE.peak_kernel(1, 1.0), True, 8.0, 13)
+    cpu_per_frame = (time.perf_counter() - t0) / 2
+    F = frames.shape[0]
+    return {"movie": f"{F} frames 512x512, 150 emitters per frame, DoG sigma 1, 13 px ROIs",
+            "rois_found": int(len(coords)), "frontend_frames_per_s": F / fe_s,
+            "frames_to_fits_frames_per_s": F / both_s,
+            "frames_to_fits_fits_per_s": len(coords) / both_s,
+            "cpu_numpy_frames_per_s": 1.0 / cpu_per_frame}
+
+
 def bench_gpu(args):
     import torch
     import bsfit
@@ -435,6 +500,7 @@ def bench_gpu(args):
         cpu_s = time.perf_counter() - t0
         prefilter_fig = {"grid": "x".join(str(g) for g in reversed(grid)) + " (Y, X, Z, W, U) float64",
                          "gpu_ms": ap.elapsed_time(bp) / 3, "cpu_numpy_ms": cpu_s * 1e3}
+    frontend_fig = None if args.no_frontend else bench_frontend(dev, stream)
     serving = None if args.no_serve else bench_serving(args, dev)
     if rank != 0:
         return 0
@@ -479,6 +545,7 @@ def bench_gpu(args):
                        "4pi_13px": fits_4pi,
                        "4pi_workload": f"{args.rois_4pi} ROIs of 4 channels 13x13, 100 iterations"},
         "prefilter": prefilter_fig,
+        "frontend": frontend_fig,
         "serving": serving,
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
@@ -504,6 +571,7 @@ def main():
     ap.add_argument("--rois-4pi", type=int, default=100000, help="ROIs of the 4Pi figure")
     ap.add_argument("--no-4pi", action="store_true")
     ap.add_argument("--no-prefilter", action="store_true")
+    ap.add_argument("--no-frontend", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-frames", type=int, default=80)
     args = ap.parse_args()

@@ -104,6 +104,24 @@ class Model:
                         L.data_ptr(), st.cuda_stream)
         return P, C, L
 
+    def fit_scmos_torch(self, rois, var, iterations, stream=None):
+        """sCMOS fit: var (same shape as rois) holds the per-pixel variance /
+        gain^2, added to model and data in the likelihood. Returns (P, CRLB,
+        LL) device tensors as fit_torch."""
+        import torch
+        assert rois.is_cuda and var.is_cuda and rois.shape == var.shape
+        r, v = rois.contiguous(), var.contiguous()
+        n, s = r.shape[0], r.shape[-1]
+        P = torch.empty((self.nv + 1, n), device=r.device, dtype=torch.float32)
+        C = torch.empty((self.nv, n), device=r.device, dtype=torch.float32)
+        L = torch.empty((n,), device=r.device, dtype=torch.float32)
+        cs = stream if stream is not None else torch.cuda.current_stream(r.device)
+        check(_native.lib().bsfit_fit_scmos_device(self._h, r.data_ptr(), v.data_ptr(), s, n,
+                                                   int(iterations), P.data_ptr(), C.data_ptr(),
+                                                   L.data_ptr(), cs.cuda_stream),
+              "bsfit_fit_scmos_device")
+        return P, C, L
+
     def fit_multistart_torch(self, rois, iterations, starts, strict=False, stream=None):
         """Fused multi-start fit (fit types 7, 8): starts is a sequence of initP
         vectors; every ROI is fitted from each and the best log-likelihood kept

@@ -611,4 +611,34 @@ int bsfit_fit4pi_multistart_device(bsfit_model model, const float* d_rois, int64
   return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
 }
 
+// ---------------------------------------------------------------------------
+// sCMOS likelihood for the B-spline fit types (the variance map, which the
+// reference's B-spline branch ignores, applied as its sCMOS kernels of the
+// other fit types do, VC/GPUmleFit_LM/GPUmleFit_LM_sCMOS.cu:1045-1046).
+
+int bsfit_fit_scmos_device(bsfit_model model, const float* d_rois, const float* d_var,
+                           int64_t roi_size, int64_t nfits, int32_t iterations, float* d_P,
+                           float* d_CRLB, float* d_LL, void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  const int ft = model->dev.fittype;
+  if (ft != 6 && ft != 7 && ft != 8) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_var || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.var = d_var;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  a.out_n = nfits;
+  return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
+}
+
 }  // extern "C"

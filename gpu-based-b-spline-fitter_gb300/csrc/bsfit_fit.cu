@@ -147,7 +147,7 @@ struct ModeTraits<8> {
 // the consecutive items of a pass (stage B writes, stage C reads) sit an odd
 // stride apart: 32 distinct banks.
 struct WarpLayout {
-  int s, s2p, wp, na, ng, nch;
+  int s, s2p, wp, na, ng, nch, nvar;  // nvar: sCMOS variance planes (0 or nch)
   bool alias;
   __host__ __device__ static constexpr int bank_pad(int x, int s) {
     return x + ((s - x) % 32 + 32) % 32;
@@ -155,7 +155,7 @@ struct WarpLayout {
   __host__ __device__ constexpr int as() const { return bank_pad(na * wp, s); }  // A column stride
   __host__ __device__ constexpr int gp() const { return ng | 1; }               // G item stride
   __host__ __device__ constexpr int gs() const { return s * gp(); }             // G column stride
-  __host__ __device__ constexpr int off_kx() const { return nch * s2p; }
+  __host__ __device__ constexpr int off_kx() const { return (nch + nvar) * s2p; }
   __host__ __device__ constexpr int off_ky() const { return off_kx() + ((s + 3) & ~3); }
   __host__ __device__ constexpr int off_w() const { return off_ky() + ((s + 3) & ~3); }
   __host__ __device__ constexpr int off_dt() const { return off_w() + 40; }
@@ -171,7 +171,7 @@ struct WarpLayout {
   __host__ __device__ constexpr int total() const { return off_maps() + maps_size(); }
 };
 
-__host__ __device__ constexpr WarpLayout make_layout(int mode, int s) {
+__host__ __device__ constexpr WarpLayout make_layout(int mode, int s, bool var = false) {
   WarpLayout L{};
   L.s = s;
   L.s2p = (s * s + 3) & ~3;
@@ -179,6 +179,7 @@ __host__ __device__ constexpr WarpLayout make_layout(int mode, int s) {
   L.na = mode == 6 ? 2 : (mode == 7 || mode == kFit4Pi) ? 3 : 8;
   L.ng = mode == 6 ? 3 : (mode == 7 || mode == kFit4Pi) ? 4 : 10;
   L.nch = mode == kFit4Pi ? k4PiChannels : 1;
+  L.nvar = var ? L.nch : 0;
   L.alias = mode == 6 || mode == 8;
   return L;
 }
@@ -190,18 +191,19 @@ __host__ __device__ constexpr WarpLayout make_layout(int mode, int s) {
 constexpr bool layouts_disjoint() {
   const int modes[4] = {6, 7, 8, kFit4Pi};
   for (int mi = 0; mi < 4; ++mi)
-    for (int s = 1; s <= 51; ++s) {
-      const WarpLayout L = make_layout(modes[mi], s);
-      if (L.nch * s * s > L.off_kx() || L.off_kx() + s > L.off_ky() ||
-          L.off_ky() + s > L.off_w() || L.off_w() + 5 * 8 > L.off_dt() ||
-          L.off_dt() + (L.nch > 1 ? L.nch * 6 : 0) > L.off_maps() ||
-          L.off_a() + L.wp * L.as() > L.total() || L.off_g() + L.wp * L.gs() > L.total())
-        return false;
-      for (int c = 0; c < L.wp; ++c)
-        if ((c + 1) * L.gs() > L.a_rel() + c * L.as()) return false;
-      if (L.as() < L.na * L.wp || L.gp() < L.ng || (L.as() - s) % 32 != 0 || L.gp() % 2 == 0)
-        return false;
-    }
+    for (int s = 1; s <= 51; ++s)
+      for (int var = 0; var < 2; ++var) {
+        const WarpLayout L = make_layout(modes[mi], s, var != 0);
+        if ((L.nch + L.nvar) * s * s > L.off_kx() || L.off_kx() + s > L.off_ky() ||
+            L.off_ky() + s > L.off_w() || L.off_w() + 5 * 8 > L.off_dt() ||
+            L.off_dt() + (L.nch > 1 ? L.nch * 6 : 0) > L.off_maps() ||
+            L.off_a() + L.wp * L.as() > L.total() || L.off_g() + L.wp * L.gs() > L.total())
+          return false;
+        for (int c = 0; c < L.wp; ++c)
+          if ((c + 1) * L.gs() > L.a_rel() + c * L.as()) return false;
+        if (L.as() < L.na * L.wp || L.gp() < L.ng || (L.as() - s) % 32 != 0 || L.gp() % 2 == 0)
+          return false;
+      }
   return true;
 }
 static_assert(layouts_disjoint(), "per-warp shared-memory regions overlap");
@@ -211,7 +213,7 @@ static_assert(make_layout(6, 13).alias == ModeTraits<6>::ALIAS &&
                   make_layout(kFit4Pi, 13).alias == ModeTraits<kFit4Pi>::ALIAS,
               "layout aliasing and stage-B synchronisation must agree");
 
-int warp_smem_floats(int mode, int s) { return make_layout(mode, s).total(); }
+int warp_smem_floats(int mode, int s, bool var) { return make_layout(mode, s, var).total(); }
 
 // ---------------------------------------------------------------------------
 // One ROI evaluation: deviance, gradient and Hessian (or Fisher information and
@@ -265,7 +267,7 @@ __device__ __forceinline__ float wrap_phase(float w, int nw) {
 // One image channel of one ROI evaluation: model and derivatives at th for
 // every pixel of `data`, accumulated into this lane's partial sums (err, and
 // acc = gradient 0 .. NV-1, packed Hessian or Fisher upper triangle NV ..).
-template <int MODE, int KP>
+template <int MODE, int KP, bool VAR>
 __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout& L, float* ws,
                                              const float* data, int lane, const float* th,
                                              bool dup45, bool FISHER, FPair& err,
@@ -660,6 +662,13 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         model = m3 * h2m + m5 * g2;
       }
       float d = data[p];
+      if constexpr (VAR) {
+        // sCMOS: variance / gain^2 added to model and data
+        // (VC/GPUmleFit_LM/GPUmleFit_LM_sCMOS.cu:1045-1046)
+        const float v = data[L.nch * L.s2p + p];
+        model += v;
+        d += v;
+      }
       const float inv = __frcp_rn(model);
       if (!FISHER) {
         // CPUmleFit_LM.cpp:2540-2559, with one reciprocal: d / m = d * (1 / m)
@@ -706,7 +715,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
 
 // Outputs are distributed over the lanes: lane l < NV receives gradient entry
 // l (gl) and Hessian row l (hr), or Fisher row l; err_out is on every lane.
-template <int MODE>
+template <int MODE, bool VAR = false>
 __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int lane,
                          const float* th, bool dup45, bool FISHER, FPair& err_out, float& gl,
                          float (&hr)[ModeTraits<MODE>::NV]) {
@@ -720,7 +729,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
 #pragma unroll
   for (int k = 0; k < KP; ++k) acc[k] = 0.0f;
   if constexpr (TR::NCH == 1) {
-    channel_pass<MODE, KP>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc);
+    channel_pass<MODE, KP, VAR>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc);
   } else {
     // 4Pi: channel c sees the shared parameters plus its offsets dT[c], with
     // its phase shifted by shift[c] and wrapped; the sums run over all
@@ -731,7 +740,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
 #pragma unroll
       for (int k = 0; k < NV; ++k) thc[k] = th[k] + dts[ch * NV + k];
       thc[5] = wrap_phase(thc[5] + a.m.shift[ch], a.m.n[3]);
-      channel_pass<MODE, KP>(a, L, ws, ws + ch * L.s2p, lane, thc, false, FISHER, err, acc);
+      channel_pass<MODE, KP, VAR>(a, L, ws, ws + ch * L.s2p, lane, thc, false, FISHER, err, acc);
     }
   }
   PHASE_DECL();
@@ -866,7 +875,7 @@ __device__ __forceinline__ float lane_solve(int lane, const float (&lr)[NV], con
 // Stage one ROI in the warp's shared memory: its pixels (4Pi: the four
 // channel planes, rois laid out [channel][roi][s][s]) and the 4Pi channel
 // offsets dT [roi][channel][6].
-template <int MODE>
+template <int MODE, bool VAR = false>
 __device__ __forceinline__ void load_roi(const FitArgs& a, const WarpLayout& L, float* ws,
                                          int lane, int64_t roi) {
   const int s2 = L.s * L.s;
@@ -875,6 +884,11 @@ __device__ __forceinline__ void load_roi(const FitArgs& a, const WarpLayout& L, 
     const float* src = a.rois + ((int64_t)ch * a.nfits + roi) * (int64_t)s2;
     float* dst = ws + ch * L.s2p;
     for (int p = lane; p < s2; p += 32) dst[p] = __ldg(src + p);
+    if constexpr (VAR) {
+      const float* vsrc = a.var + ((int64_t)ch * a.nfits + roi) * (int64_t)s2;
+      float* vdst = ws + (nch + ch) * L.s2p;
+      for (int p = lane; p < s2; p += 32) vdst[p] = __ldg(vsrc + p);
+    }
   }
   if constexpr (ModeTraits<MODE>::NCH > 1) {
     constexpr int ND = ModeTraits<MODE>::NCH * ModeTraits<MODE>::NV;
@@ -941,7 +955,7 @@ struct RoiResult {
 
 // Fit of the ROI staged in ws (load_roi) from start `start` (0 unless
 // multi-start).
-template <int MODE>
+template <int MODE, bool VAR = false>
 __device__ RoiResult fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int lane, int64_t roi,
                              int start) {
   using TR = ModeTraits<MODE>;
@@ -1022,7 +1036,7 @@ __device__ RoiResult fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, i
 #pragma unroll
       for (int k = 0; k < NV; ++k)
         the[k] = bcast((MODE == 8 && fisher && k != 2 && k != 3) ? par_eval : par, k);
-      evaluate<MODE>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr);
+      evaluate<MODE, VAR>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr);
       first = false;
       need_eval = false;
       if (fisher) {
@@ -1336,10 +1350,10 @@ __device__ __forceinline__ void store_result(const FitArgs& a, int lane, int64_t
 // demo_orientation/store/fitb5n3.m:36-45, demo_4pi/bspline_based_4piloc_v4.m:201-214).
 // MULTI selects the multi-start kernels; the single-start ones carry no start
 // loop (it would cost them registers).
-template <int MODE, bool MULTI>
+template <int MODE, bool MULTI, bool VAR = false>
 __device__ __forceinline__ void fit_and_store(const FitArgs& a, const WarpLayout& L, float* ws,
                                               int lane, int64_t roi) {
-  load_roi<MODE>(a, L, ws, lane, roi);
+  load_roi<MODE, VAR>(a, L, ws, lane, roi);
   if constexpr (MULTI) {
     // one call site for all starts (a second inlined copy of the fit would
     // double the kernel's instruction footprint)
@@ -1351,22 +1365,22 @@ __device__ __forceinline__ void fit_and_store(const FitArgs& a, const WarpLayout
     }
     store_result<MODE>(a, lane, roi, best);
   } else {
-    store_result<MODE>(a, lane, roi, fit_roi<MODE>(a, L, ws, lane, roi, 0));
+    store_result<MODE>(a, lane, roi, fit_roi<MODE, VAR>(a, L, ws, lane, roi, 0));
   }
 }
 
-template <int MODE, bool MULTI>
+template <int MODE, bool MULTI, bool VAR = false>
 __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) fit_kernel(FitArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
-  const WarpLayout L = make_layout(MODE, a.s);
+  const WarpLayout L = make_layout(MODE, a.s, VAR);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   float* ws = smem + wib * L.total();
   const int64_t total_warps = (int64_t)gridDim.x * wpb;
   for (int64_t roi = (int64_t)blockIdx.x * wpb + wib; roi < a.nfits; roi += total_warps)
-    fit_and_store<MODE, MULTI>(a, L, ws, lane, roi);
+    fit_and_store<MODE, MULTI, VAR>(a, L, ws, lane, roi);
 }
 
 // Persistent batched fit: every warp claims ROIs one at a time from the
@@ -1410,6 +1424,7 @@ __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) batch_kernel(const
     fa.w0 = nullptr;
     fa.n_starts = 0;
     fa.strict = 0;
+    fa.var = nullptr;
     fit_and_store<MODE, false>(fa, make_layout(MODE, g.s), ws, lane, (int64_t)i);
     if (lane == 0) atomicAdd(&a.done[g.slot], 1ull);
   }
@@ -1567,13 +1582,15 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
   }
   const int mode = a.m.fittype;
-  const int per_warp = warp_smem_floats(mode, a.s) * 4;
+  const bool var = a.var != nullptr;
+  const int per_warp = warp_smem_floats(mode, a.s, var) * 4;
   void (*kern)(FitArgs) = nullptr;
   const bool multi = a.n_starts > 1;
-  if (mode == 6) kern = fit_kernel<6, false>;
-  else if (mode == 7) kern = multi ? fit_kernel<7, true> : fit_kernel<7, false>;
-  else if (mode == 8) kern = multi ? fit_kernel<8, true> : fit_kernel<8, false>;
-  else if (mode == kFit4Pi) kern = multi ? fit_kernel<kFit4Pi, true> : fit_kernel<kFit4Pi, false>;
+  if (var && multi) return cudaErrorInvalidValue;  // not combined
+  if (mode == 6) kern = var ? fit_kernel<6, false, true> : fit_kernel<6, false>;
+  else if (mode == 7) kern = var ? fit_kernel<7, false, true> : multi ? fit_kernel<7, true> : fit_kernel<7, false>;
+  else if (mode == 8) kern = var ? fit_kernel<8, false, true> : multi ? fit_kernel<8, true> : fit_kernel<8, false>;
+  else if (mode == kFit4Pi && !var) kern = multi ? fit_kernel<kFit4Pi, true> : fit_kernel<kFit4Pi, false>;
   else return cudaErrorInvalidValue;
   // Warps per block: the choice among 4, 2, 1 that keeps the most warps
   // resident per SM (shared memory per warp grows with s and the model).

@@ -54,6 +54,9 @@ struct FitArgs {
   int n_starts;
   int strict;
   float starts[8][4];
+  // sCMOS: per-pixel variance / gain^2 in the ROI layout, added to model and
+  // data in the likelihood (null: EMCCD)
+  const float* var;
 };
 
 constexpr int kMaxStarts = 8;
@@ -87,7 +90,7 @@ struct BatchArgs {
   BatchSeg seg[kMaxBatchSegs];
 };
 
-int warp_smem_floats(int mode, int s);
+int warp_smem_floats(int mode, int s, bool var = false);
 cudaError_t launch_batch(const BatchArgs& a, int mode, cudaStream_t stream);
 cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream);
 cudaError_t measure_fp32_peak(double* tflops);

@@ -344,6 +344,19 @@ int bsfit_bsarray_coeffs_device(const double* d_samples, int32_t ndim, const int
 int bsfit_bsarray_coeffs(const double* samples, int32_t ndim, const int64_t* dims, float* coeff);
 
 /*
+ * sCMOS likelihood for fit types 6, 7, 8 (no reference counterpart: the
+ * reference's B-spline branch ignores its variance map; its sCMOS kernels of
+ * the Gaussian and cubic-spline fit types add the per-pixel variance / gain^2
+ * to both model and data, VC/GPUmleFit_LM/GPUmleFit_LM_sCMOS.cu:1045-1046, and
+ * this applies the same to the B-spline likelihood). d_var: variance / gain^2
+ * in the ROI layout ([nfits][s][s]); outputs as bsfit_fit_device. The drop-in
+ * call bsfit_GPUmleFit_LM_multiD keeps ignoring varmap, as the reference does.
+ */
+int bsfit_fit_scmos_device(bsfit_model model, const float* d_rois, const float* d_var,
+                           int64_t roi_size, int64_t nfits, int32_t iterations, float* d_P,
+                           float* d_CRLB, float* d_LL, void* stream);
+
+/*
  * Frame -> ROI front end (the step before the fit in the reference's
  * acquisition loop, MultiD_fitter/simplefitter_cspline.m:197-319, with the peak
  * finder MultiD_fitter/shared/maximumfind2.c): photon conversion, filtering,

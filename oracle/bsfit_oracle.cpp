@@ -510,9 +510,12 @@ struct Model53D {
 enum Mode { MODE6 = 6, MODE7 = 7, MODE8 = 8 };
 
 // One ROI evaluation at the current theta: deviance, gradient and Hessian.
+// s_var (sCMOS, may be null): per-pixel variance / gain^2 added to both model
+// and data, as the reference's sCMOS kernels do for the other fit types
+// (VC/GPUmleFit_LM/GPUmleFit_LM_sCMOS.cu:1045-1046, :1206-1207).
 template <typename T, typename MDL>
 void eval_roi(MDL& mdl, int sz, const T* s_data, const T* theta, bool pow_double, bool dup_dudt45,
-              T* err, T* jac, T* hes) {
+              T* err, T* jac, T* hes, const T* s_var = nullptr) {
   constexpr int NV = MDL::NV;
   *err = 0;
   std::memset(jac, 0, NV * sizeof(T));
@@ -524,6 +527,10 @@ void eval_roi(MDL& mdl, int sz, const T* s_data, const T* theta, bool pow_double
       T model;
       mdl.pixel(ii, jj, theta, dudt, &model);
       T data = s_data[sz * jj + ii];
+      if (s_var) {
+        model += s_var[sz * jj + ii];
+        data += s_var[sz * jj + ii];
+      }
       if (dup_dudt45) dudt[5] = dudt[4];
       accumulate_pixel<T>(model, data, dudt, NV, pow_double, err, jac, hes);
     }
@@ -538,10 +545,11 @@ constexpr int TRACE_REC = 32;
 template <typename T, typename MDL, Mode MODE>
 void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, const T* initP,
              T* d_Parameters, T* d_CRLBs, T* d_LogLikelihood, int Nfits,
-             double* trace = nullptr, int trace_max = 0) {
+             double* trace = nullptr, int trace_max = 0, const T* d_var = nullptr) {
   constexpr int NV = MDL::NV;
   const int* n = mdl.n;
   const T* s_data = d_data + (long long)sz * sz * subregion;
+  const T* s_var = d_var ? d_var + (long long)sz * sz * subregion : nullptr;
 
   T newTheta[NV + 1], oldTheta[NV + 1];
   T newLambda = 1.0, oldLambda = 1.0;
@@ -603,8 +611,8 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
 
   // Initial evaluation. Mode 7 copies dudt[4] into dudt[5] here only (:2893);
   // mode 8 uses float pow here only (:3320).
-  eval_roi<T>(mdl, sz, s_data, newTheta, MODE != MODE8, MODE == MODE7, &newErr, jacobian,
-              hessian);
+  eval_roi<T>(mdl, sz, s_data, newTheta, MODE != MODE8, MODE == MODE7, &newErr, jacobian, hessian,
+              s_var);
 
   int kk;
   for (kk = 0; kk < iterations; kk++) {
@@ -736,7 +744,7 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
         newTheta[7] = mmin(newTheta[7], (T)1);
         newTheta[7] = mmax(newTheta[7], (T)0);
       }
-      eval_roi<T>(mdl, sz, s_data, newTheta, true, false, &newErr, jacobian, hessian);
+      eval_roi<T>(mdl, sz, s_data, newTheta, true, false, &newErr, jacobian, hessian, s_var);
     } else {
       newLambda = 10 * newLambda;
     }
@@ -768,6 +776,10 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
       T model;
       mdl.pixel(ii, jj, newTheta, dudt, &model);
       T data = s_data[sz * jj + ii];
+      if (s_var) {
+        model += s_var[sz * jj + ii];
+        data += s_var[sz * jj + ii];
+      }
       accumulate_fisher<T>(model, data, dudt, NV, M, &Div);
     }
   mat_inv_n<T>(M, Minv, Diag, NV);
@@ -779,7 +791,7 @@ void fit_roi(MDL& mdl, int subregion, const T* d_data, int sz, int iterations, c
 
 template <typename T>
 void fit6(const T* data, const T* coeff, int cx, int cy, int cz, int sz, int iterations,
-          int nfits, T* P, T* CRLB, T* LL, int threads) {
+          int nfits, T* P, T* CRLB, T* LL, int threads, const T* var = nullptr) {
 #pragma omp parallel for schedule(dynamic, 64) num_threads(threads > 0 ? threads : 1)
   for (int i = 0; i < nfits; i++) {
     Model3D<T> m;
@@ -789,13 +801,14 @@ void fit6(const T* data, const T* coeff, int cx, int cy, int cz, int sz, int ite
     m.n[0] = cy - 3;
     m.n[1] = cx - 3;
     m.n[2] = cz - 3;
-    fit_roi<T, Model3D<T>, MODE6>(m, i, data, sz, iterations, nullptr, P, CRLB, LL, nfits);
+    fit_roi<T, Model3D<T>, MODE6>(m, i, data, sz, iterations, nullptr, P, CRLB, LL, nfits, nullptr,
+                                  0, var);
   }
 }
 
 template <typename T>
 void fit7(const T* data, const T* coeff, int cx, int cy, int cz, int cw, int sz, int iterations,
-          const T* initP, int nfits, T* P, T* CRLB, T* LL, int threads) {
+          const T* initP, int nfits, T* P, T* CRLB, T* LL, int threads, const T* var = nullptr) {
 #pragma omp parallel for schedule(dynamic, 64) num_threads(threads > 0 ? threads : 1)
   for (int i = 0; i < nfits; i++) {
     Model4D<T>* m = new Model4D<T>;
@@ -804,14 +817,16 @@ void fit7(const T* data, const T* coeff, int cx, int cy, int cz, int cw, int sz,
     m->n[1] = cx - 3;
     m->n[2] = cz - 3;
     m->n[3] = cw - 3;
-    fit_roi<T, Model4D<T>, MODE7>(*m, i, data, sz, iterations, initP, P, CRLB, LL, nfits);
+    fit_roi<T, Model4D<T>, MODE7>(*m, i, data, sz, iterations, initP, P, CRLB, LL, nfits, nullptr, 0,
+                                  var);
     delete m;
   }
 }
 
 template <typename T>
 void fit8(const T* data, const T* coeff5, const T* coeff3, int cx, int cy, int cz, int cw, int cu,
-          int sz, int iterations, const T* initP, int nfits, T* P, T* CRLB, T* LL, int threads) {
+          int sz, int iterations, const T* initP, int nfits, T* P, T* CRLB, T* LL, int threads,
+          const T* var = nullptr) {
 #pragma omp parallel for schedule(dynamic, 16) num_threads(threads > 0 ? threads : 1)
   for (int i = 0; i < nfits; i++) {
     Model53D<T>* m = new Model53D<T>;
@@ -822,7 +837,8 @@ void fit8(const T* data, const T* coeff5, const T* coeff3, int cx, int cy, int c
     m->n[2] = cz - 3;
     m->n[3] = cw - 3;
     m->n[4] = cu - 3;
-    fit_roi<T, Model53D<T>, MODE8>(*m, i, data, sz, iterations, initP, P, CRLB, LL, nfits);
+    fit_roi<T, Model53D<T>, MODE8>(*m, i, data, sz, iterations, initP, P, CRLB, LL, nfits, nullptr,
+                                   0, var);
     delete m;
   }
 }
@@ -1287,5 +1303,45 @@ void oracle_eval4pi_f64(const double* imstack, const double* coeff, const int* c
       for (int m = l; m < NV; ++m) o[1 + NV + k++] = hes[l * NV + m];
   }
   delete[] chm;
+}
+}  // extern "C"
+
+extern "C" {
+// sCMOS variants: var holds the per-pixel variance / gain^2 in the ROI layout
+// (restated from the reference's sCMOS kernels of the other fit types; the
+// reference's B-spline fit types ignore the variance map).
+void oracle_fit6_scmos_f64(const double* data, const double* var, const double* coeff, int cx,
+                           int cy, int cz, int sz, int iterations, int nfits, double* P,
+                           double* CRLB, double* LL, int threads) {
+  fit6<double>(data, coeff, cx, cy, cz, sz, iterations, nfits, P, CRLB, LL, threads, var);
+}
+void oracle_fit6_scmos_f32(const float* data, const float* var, const float* coeff, int cx, int cy,
+                           int cz, int sz, int iterations, int nfits, float* P, float* CRLB,
+                           float* LL, int threads) {
+  fit6<float>(data, coeff, cx, cy, cz, sz, iterations, nfits, P, CRLB, LL, threads, var);
+}
+void oracle_fit7_scmos_f64(const double* data, const double* var, const double* coeff, int cx,
+                           int cy, int cz, int cw, int sz, int iterations, const double* initP,
+                           int nfits, double* P, double* CRLB, double* LL, int threads) {
+  fit7<double>(data, coeff, cx, cy, cz, cw, sz, iterations, initP, nfits, P, CRLB, LL, threads, var);
+}
+void oracle_fit7_scmos_f32(const float* data, const float* var, const float* coeff, int cx, int cy,
+                           int cz, int cw, int sz, int iterations, const float* initP, int nfits,
+                           float* P, float* CRLB, float* LL, int threads) {
+  fit7<float>(data, coeff, cx, cy, cz, cw, sz, iterations, initP, nfits, P, CRLB, LL, threads, var);
+}
+void oracle_fit8_scmos_f64(const double* data, const double* var, const double* coeff5,
+                           const double* coeff3, int cx, int cy, int cz, int cw, int cu, int sz,
+                           int iterations, const double* initP, int nfits, double* P, double* CRLB,
+                           double* LL, int threads) {
+  fit8<double>(data, coeff5, coeff3, cx, cy, cz, cw, cu, sz, iterations, initP, nfits, P, CRLB, LL,
+               threads, var);
+}
+void oracle_fit8_scmos_f32(const float* data, const float* var, const float* coeff5,
+                           const float* coeff3, int cx, int cy, int cz, int cw, int cu, int sz,
+                           int iterations, const float* initP, int nfits, float* P, float* CRLB,
+                           float* LL, int threads) {
+  fit8<float>(data, coeff5, coeff3, cx, cy, cz, cw, cu, sz, iterations, initP, nfits, P, CRLB, LL,
+              threads, var);
 }
 }  // extern "C"

@@ -26,7 +26,8 @@ def _ptr(a, dt):
 
 
 class _Base:
-    def _call(self, fn_name, dt, rois, fittype, iterations, coeff, init_p, coeff3, threads):
+    def _call(self, fn_name, dt, rois, fittype, iterations, coeff, init_p, coeff3, threads,
+              var=None):
         rois = np.ascontiguousarray(rois, dtype=dt)
         if rois.ndim == 2:
             rois = rois[None]
@@ -38,7 +39,12 @@ class _Base:
         C = np.zeros((nv, n), dtype=dt)
         L = np.zeros(n, dtype=dt)
         fn = getattr(self.lib(dt), fn_name)
-        args = [_ptr(rois, dt), _ptr(coeff, dt)]
+        args = [_ptr(rois, dt)]
+        if var is not None:
+            v = np.ascontiguousarray(var, dtype=dt)
+            assert v.shape == rois.shape
+            args.append(_ptr(v, dt))
+        args.append(_ptr(coeff, dt))
         if fittype == 8:
             c3 = np.ascontiguousarray(coeff3, dtype=dt)
             args.append(_ptr(c3, dt))
@@ -74,8 +80,12 @@ class Oracle(_Base):
         return self._lib
 
     def fit(self, rois, fittype, iterations, coeff, init_p=None, coeff3=None, precision="f32",
-            threads=1):
+            threads=1, var=None):
+        """var: sCMOS per-pixel variance / gain^2 (same shape as rois), or None."""
         dt = np.float32 if precision == "f32" else np.float64
+        if var is not None:
+            return self._call(f"oracle_fit{fittype}_scmos_{precision}", dt, rois, fittype,
+                              iterations, coeff, init_p, coeff3, threads, var=var)
         return self._call(f"oracle_fit{fittype}_{precision}", dt, rois, fittype, iterations, coeff,
                           init_p, coeff3, threads)
 

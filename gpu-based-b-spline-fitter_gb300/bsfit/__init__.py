@@ -31,8 +31,14 @@ def _dims(a):
 
 
 def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, silent=1,
-                        initP=None, coeff3=None):
-    """Drop-in for the reference mex (fit types 6, 7, 8); raises BsfitError."""
+                        initP=None, coeff3=None, out=None):
+    """Drop-in for the reference mex (fit types 6, 7, 8); raises BsfitError.
+
+    Returns (P, CRLB, LL) shaped (N, NV + 1), (N, NV), (N,): views of the C
+    ABI's column-major outputs (no copy). out=(P, CRLB, LL) passes caller-owned
+    float32 buffers in the C ABI's layout ((NV + 1, N), (NV, N), (N,)), which
+    are filled and returned as the same views, as a host application calling
+    the C ABI directly would reuse its buffers."""
     lib = _native.lib()
     im = _f32(imstack)
     if im.ndim == 2:
@@ -46,9 +52,14 @@ def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, s
     c3 = _f32(coeff3) if coeff3 is not None else None
     ip = _f32(np.atleast_1d(initP)) if initP is not None else None
     vm = _f32(np.atleast_1d(varmap)) if varmap is not None else None
-    P = np.zeros((max(nv, 1) + 1, n), np.float32)
-    C = np.zeros((max(nv, 1), n), np.float32)
-    L = np.zeros(n, np.float32)
+    if out is None:
+        P = np.empty((max(nv, 1) + 1, n), np.float32)
+        C = np.empty((max(nv, 1), n), np.float32)
+        L = np.empty(n, np.float32)
+    else:
+        P, C, L = out
+        assert P.shape == (nv + 1, n) and C.shape == (nv, n) and L.shape == (n,)
+        assert all(x.dtype == np.float32 and x.flags.c_contiguous for x in (P, C, L))
     ptr = lambda a: a.ctypes.data_as(_fp) if a is not None else None  # noqa: E731
     st = lib.bsfit_GPUmleFit_LM_multiD(
         ptr(im), s1, s2, n, fittype, int(iterations),
@@ -58,7 +69,7 @@ def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, s
         ptr(c3), c3.ndim if c3 is not None else 0, _dims(c3) if c3 is not None else None,
         ptr(P), ptr(C), ptr(L))
     check(st, "GPUmleFit_LM_multiD")
-    return P.T.copy(), C.T.copy(), L
+    return P.T, C.T, L
 
 
 class Model:
@@ -203,9 +214,9 @@ def GPUmleFit_LM_4Pi_bspline(imstack, shared, iterations, coeff, dT, initZ, init
     z0 = _f32(np.atleast_1d(initZ))
     w0 = _f32(np.atleast_1d(initPhi))
     ps = _f32(np.atleast_1d(phase_shift))
-    P = np.zeros((7, n), np.float32)
-    C = np.zeros((6, n), np.float32)
-    L = np.zeros(n, np.float32)
+    P = np.empty((7, n), np.float32)
+    C = np.empty((6, n), np.float32)
+    L = np.empty(n, np.float32)
     ptr = lambda a: a.ctypes.data_as(_fp)  # noqa: E731
     st = lib.bsfit_GPUmleFit_LM_4Pi_bspline(
         ptr(im), s1, s2, n, ch, sh.ctypes.data_as(np.ctypeslib.ctypes.POINTER(
@@ -213,7 +224,7 @@ def GPUmleFit_LM_4Pi_bspline(imstack, shared, iterations, coeff, dT, initZ, init
         ptr(dt), dt.size, ptr(z0), z0.size, ptr(w0), w0.size, ptr(ps), ps.size, int(silent),
         ptr(P), ptr(C), ptr(L))
     check(st, "GPUmleFit_LM_4Pi_bspline")
-    return P.T.copy(), C.T.copy(), L
+    return P.T, C.T, L
 
 
 class Model4Pi:

@@ -6,6 +6,7 @@
 // device is ever reset. Device buffers of the plain call come from the
 // stream-ordered allocator, so repeated calls reuse pooled memory instead of
 // allocating and freeing per call as the reference does.
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -84,6 +85,74 @@ int cuda_status(cudaError_t e) {
   return BSFIT_E_CUDA;
 }
 
+// Argument checks of a model (shared by bsfit_model_create and the drop-in
+// call, which builds its model on a stream instead).
+int check_model_args(int fittype, const float* coeff, int ndim, const int64_t* dims,
+                     const float* coeff3, int ndim3, const int64_t* dims3, const float* init_p,
+                     int64_t init_p_numel) {
+  if (num_params(fittype) == 0) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (!coeff) return BSFIT_E_WRONG_DATA_TYPE;
+  int st = check_coeff(fittype, ndim, dims);
+  if (st) return st;
+  if (fittype == 7 && (!init_p || init_p_numel < 2)) return BSFIT_E_INIT_P;
+  if (fittype == 8) {
+    // The reference leaves g2 uninitialised without initP (CPUmleFit_LM.cpp:3246-3256).
+    if (!init_p || init_p_numel < 4) return BSFIT_E_INIT_P;
+    if (!coeff3 || !dims3 || ndim3 != 3) return BSFIT_E_WRONG_DATA_TYPE;
+    for (int i = 0; i < 3; ++i)
+      if (dims3[i] != dims[i]) return BSFIT_E_COEFF_SIZE;
+  }
+  return BSFIT_OK;
+}
+
+// Streams and events of the synchronous drop-in call, created once per host
+// thread and device (the call is synchronous, so a thread never has two in
+// flight).
+struct CallStreams {
+  static constexpr int kEvents = 8;
+  int device = -1;
+  cudaStream_t copy = nullptr, comp[2] = {nullptr, nullptr};
+  cudaEvent_t ev[kEvents] = {}, join = nullptr;
+  ~CallStreams() { release(); }
+  void release() {
+    if (device < 0) return;
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess) return;  // runtime already gone
+    for (auto* st : {&copy, &comp[0], &comp[1]})
+      if (*st) cudaStreamDestroy(*st);
+    for (auto& x : ev)
+      if (x) cudaEventDestroy(x);
+    if (join) cudaEventDestroy(join);
+    device = -1;
+  }
+};
+
+CallStreams* call_streams() {
+  static thread_local CallStreams cs;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  if (cs.device == dev) return &cs;
+  cs.release();
+  bool ok = cudaStreamCreateWithFlags(&cs.copy, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&cs.comp[0], cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&cs.comp[1], cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&cs.join, cudaEventDisableTiming) == cudaSuccess;
+  for (auto& x : cs.ev) ok = ok && cudaEventCreateWithFlags(&x, cudaEventDisableTiming) == cudaSuccess;
+  // Keep freed blocks of this process's default pool cached instead of
+  // returning them at every synchronisation, so repeated calls reuse them.
+  cudaMemPool_t pool = nullptr;
+  if (ok && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cs.device = dev;
+  if (!ok) {
+    cs.release();
+    return nullptr;
+  }
+  return &cs;
+}
+
 }  // namespace
 
 extern "C" {
@@ -127,18 +196,9 @@ int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
                        bsfit_model* out) {
   if (!out) return BSFIT_E_INVALID;
   *out = nullptr;
-  if (num_params(fittype) == 0) return BSFIT_E_UNSUPPORTED_FITTYPE;
-  if (!coeff) return BSFIT_E_WRONG_DATA_TYPE;
-  int st = check_coeff(fittype, coeff_ndim, coeff_dims);
+  int st = check_model_args(fittype, coeff, coeff_ndim, coeff_dims, coeff3, coeff3_ndim,
+                            coeff3_dims, init_p, init_p_numel);
   if (st) return st;
-  if (fittype == 7 && (!init_p || init_p_numel < 2)) return BSFIT_E_INIT_P;
-  if (fittype == 8) {
-    // The reference leaves g2 uninitialised without initP (CPUmleFit_LM.cpp:3246-3256).
-    if (!init_p || init_p_numel < 4) return BSFIT_E_INIT_P;
-    if (!coeff3 || !coeff3_dims || coeff3_ndim != 3) return BSFIT_E_WRONG_DATA_TYPE;
-    for (int i = 0; i < 3; ++i)
-      if (coeff3_dims[i] != coeff_dims[i]) return BSFIT_E_COEFF_SIZE;
-  }
   bsfit_model_s* m = new (std::nothrow) bsfit_model_s;
   if (!m) return BSFIT_E_NOT_ENOUGH_MEMORY;
   fill_model(m->dev, fittype, coeff_dims, init_p, init_p_numel);
@@ -332,46 +392,83 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
     std::printf("subregion size: %lld fittype: %d\n", (long long)roi_size, fittype);
     std::printf("Number of fits: %lld no padding\n", (long long)nfits);
   }
-  bsfit_model model = nullptr;
-  int st = bsfit_model_create(fittype, coeff, coeff_ndim, coeff_dims, coeff3, coeff3_ndim,
-                              coeff3_dims, init_p, init_p_numel, &model);
+  int st = check_model_args(fittype, coeff, coeff_ndim, coeff_dims, coeff3, coeff3_ndim,
+                            coeff3_dims, init_p, init_p_numel);
   if (st) return st;
-  if (nfits == 0) {
-    bsfit_model_release(model);
-    return BSFIT_OK;
-  }
+  if (nfits == 0) return BSFIT_OK;
   // Memory check (mex :409-456): refuse work above 95% of free memory.
   const size_t s2 = (size_t)roi_size * roi_size;
   const size_t in_bytes = (size_t)nfits * s2 * sizeof(float);
   const size_t out_bytes = (size_t)nfits * (2 * nv + 2) * sizeof(float);
+  const size_t c_bytes = (size_t)numel(coeff_ndim, coeff_dims) * sizeof(float);
+  const size_t c3_bytes = fittype == 8 ? (size_t)numel(3, coeff3_dims) * sizeof(float) : 0;
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
-      (double)(in_bytes + out_bytes) > 0.95 * (double)free_b) {
-    bsfit_model_release(model);
+      (double)(in_bytes + out_bytes + c_bytes + c3_bytes) > 0.95 * (double)free_b)
     return BSFIT_E_NOT_ENOUGH_MEMORY;
+  // Pipeline: a copy stream uploads the coefficients and the ROIs chunk by
+  // chunk; two compute streams fit the chunks alternately as their uploads
+  // land, so chunk i + 1 uploads while chunk i fits and the tail of one fit
+  // launch overlaps the start of the next. Results come back in one copy at the
+  // end (the outputs are column-major over all ROIs). Device buffers come from
+  // the stream-ordered pool, so repeated calls allocate nothing.
+  CallStreams* cs = call_streams();
+  if (!cs) return BSFIT_E_CUDA;
+  cudaStream_t cp = cs->copy, c0 = cs->comp[0], c1 = cs->comp[1];
+  const int64_t chunk_min = 131072;
+  const int64_t nchunk = std::min<int64_t>(CallStreams::kEvents, std::max<int64_t>(1, nfits / chunk_min));
+  const int64_t chunk = (nfits + nchunk - 1) / nchunk;
+  float *d_rois = nullptr, *d_out = nullptr, *d_c = nullptr, *d_c3 = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_rois, in_bytes, cp);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_out, out_bytes, cp);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_c, c_bytes, cp);
+  if (e == cudaSuccess && c3_bytes) e = cudaMallocAsync(&d_c3, c3_bytes, cp);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, coeff, c_bytes, cudaMemcpyHostToDevice, cp);
+  if (e == cudaSuccess && c3_bytes)
+    e = cudaMemcpyAsync(d_c3, coeff3, c3_bytes, cudaMemcpyHostToDevice, cp);
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  fill_model(a.m, fittype, coeff_dims, init_p, init_p_numel);
+  a.m.coeff = d_c;
+  a.m.coeff3 = d_c3;
+  a.s = (int)roi_size;
+  a.iterations = iterations;
+  a.P = d_out;
+  a.CRLB = d_out + (size_t)nfits * (nv + 1);
+  a.LL = a.CRLB + (size_t)nfits * nv;
+  a.out_n = nfits;
+  for (int64_t i = 0; i < nchunk && e == cudaSuccess; ++i) {
+    const int64_t b = i * chunk, n = std::min(chunk, nfits - b);
+    if (n <= 0) break;
+    e = cudaMemcpyAsync(d_rois + (size_t)b * s2, imstack + (size_t)b * s2, (size_t)n * s2 * 4,
+                        cudaMemcpyHostToDevice, cp);
+    if (e == cudaSuccess) e = cudaEventRecord(cs->ev[i], cp);
+    cudaStream_t cs_i = (i & 1) ? c1 : c0;
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs_i, cs->ev[i], 0);
+    if (e == cudaSuccess) {
+      a.rois = d_rois + (size_t)b * s2;
+      a.nfits = n;
+      a.out_offset = b;
+      e = bsfit::launch_fit(a, cs_i);
+    }
   }
-  cudaStream_t stream = nullptr;
-  cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
-  float *d_rois = nullptr, *d_out = nullptr;
-  if (e == cudaSuccess) e = cudaMallocAsync(&d_rois, in_bytes, stream);
-  if (e == cudaSuccess) e = cudaMallocAsync(&d_out, out_bytes, stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rois, imstack, in_bytes, cudaMemcpyHostToDevice, stream);
-  float* d_P = d_out;
-  float* d_C = d_P + (size_t)nfits * (nv + 1);
-  float* d_L = d_C + (size_t)nfits * nv;
-  if (e == cudaSuccess) {
-    st = bsfit_fit_device(model, d_rois, roi_size, nfits, iterations, d_P, d_C, d_L, stream);
-    if (st) e = cudaErrorUnknown;
-  }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(P, d_P, (size_t)nfits * (nv + 1) * sizeof(float), cudaMemcpyDeviceToHost, stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(CRLB, d_C, (size_t)nfits * nv * sizeof(float), cudaMemcpyDeviceToHost, stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(LL, d_L, (size_t)nfits * sizeof(float), cudaMemcpyDeviceToHost, stream);
-  if (d_rois) cudaFreeAsync(d_rois, stream);
-  if (d_out) cudaFreeAsync(d_out, stream);
-  cudaError_t e2 = stream ? cudaStreamSynchronize(stream) : cudaSuccess;
-  if (stream) cudaStreamDestroy(stream);
-  bsfit_model_release(model);
-  if (st) return st;
+  // join: c0 waits for c1's last launch, then copies the results back
+  if (e == cudaSuccess) e = cudaEventRecord(cs->join, c1);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c0, cs->join, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P, a.P, (size_t)nfits * (nv + 1) * sizeof(float), cudaMemcpyDeviceToHost, c0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(CRLB, a.CRLB, (size_t)nfits * nv * sizeof(float), cudaMemcpyDeviceToHost, c0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(LL, a.LL, (size_t)nfits * sizeof(float), cudaMemcpyDeviceToHost, c0);
+  // buffers were allocated on the copy stream: free them on c0 once the copy
+  // stream's work is ordered before it (the chunk events already are)
+  if (cudaEventRecord(cs->join, cp) == cudaSuccess) cudaStreamWaitEvent(c0, cs->join, 0);
+  if (d_rois) cudaFreeAsync(d_rois, c0);
+  if (d_out) cudaFreeAsync(d_out, c0);
+  if (d_c) cudaFreeAsync(d_c, c0);
+  if (d_c3) cudaFreeAsync(d_c3, c0);
+  cudaError_t e2 = cudaStreamSynchronize(c0);
   if (e == cudaSuccess) e = e2;
   return cuda_status(e);
 }

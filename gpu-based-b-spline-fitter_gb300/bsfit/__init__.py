@@ -133,6 +133,29 @@ class Model:
               "bsfit_fit_scmos_device")
         return P, C, L
 
+    def fit_f64_torch(self, rois, iterations, var=None, stream=None):
+        """FP64 reference-precision fit (fit types 6, 7, 8): the reference's
+        method in double with its order of operations. rois: float32 device
+        tensor (N, s, s); var: optional sCMOS variance of the same shape.
+        Returns (P (NV+1, N), CRLB (NV, N), LL (N,)) float64 device tensors."""
+        import torch
+        assert rois.is_cuda and rois.dtype == torch.float32
+        r = rois.contiguous()
+        v = None
+        if var is not None:
+            assert var.is_cuda and var.dtype == torch.float32 and var.shape == rois.shape
+            v = var.contiguous()
+        n, s = r.shape[0], r.shape[-1]
+        P = torch.empty((self.nv + 1, n), device=r.device, dtype=torch.float64)
+        C = torch.empty((self.nv, n), device=r.device, dtype=torch.float64)
+        L = torch.empty((n,), device=r.device, dtype=torch.float64)
+        cs = stream if stream is not None else torch.cuda.current_stream(r.device)
+        check(_native.lib().bsfit_fit_f64_device(
+            self._h, r.data_ptr(), v.data_ptr() if v is not None else None, s, n,
+            int(iterations), P.data_ptr(), C.data_ptr(), L.data_ptr(), cs.cuda_stream),
+            "bsfit_fit_f64_device")
+        return P, C, L
+
     def fit_multistart_torch(self, rois, iterations, starts, strict=False, stream=None):
         """Fused multi-start fit (fit types 7, 8): starts is a sequence of initP
         vectors; every ROI is fitted from each and the best log-likelihood kept

@@ -13,6 +13,9 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libbsfit.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+# Per-file flags: the FP64 reference-precision fitter follows a build without
+# floating-point contraction.
+FILE_FLAGS = {"bsfit_fit64.cu": ["-fmad=false"]}
 
 
 def sources():
@@ -37,7 +40,8 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(LIBDIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc, *ARCH, *FLAGS, "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-c", src,
+               "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "../../include/bsfit.h"
@@ -22,6 +23,10 @@ struct bsfit_model_s {
   ModelDev dev;
   float* d_coeff = nullptr;
   float* d_coeff3 = nullptr;
+  // Double copies for the FP64 reference-precision fit, made on first use.
+  double* d_coeff64 = nullptr;
+  double* d_coeff3_64 = nullptr;
+  std::mutex f64_mu;
 };
 
 namespace {
@@ -228,6 +233,8 @@ int bsfit_model_release(bsfit_model model) {
   if (!model) return BSFIT_E_INVALID;
   cudaFree(model->d_coeff);
   cudaFree(model->d_coeff3);
+  cudaFree(model->d_coeff64);
+  cudaFree(model->d_coeff3_64);
   delete model;
   return BSFIT_OK;
 }
@@ -736,6 +743,65 @@ int bsfit_fit_scmos_device(bsfit_model model, const float* d_rois, const float* 
   a.LL = d_LL;
   a.out_n = nfits;
   return cuda_status(bsfit::launch_fit(a, (cudaStream_t)stream));
+}
+
+// ---------------------------------------------------------------------------
+// FP64 reference-precision fit: the reference method in double with its order
+// of operations (the float build of the reference and the FP32 kernels take
+// some LM decisions differently from the double build; this one follows it).
+
+int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_var,
+                         int64_t roi_size, int64_t nfits, int32_t iterations, double* d_P,
+                         double* d_CRLB, double* d_LL, void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  const int ft = model->dev.fittype;
+  if (ft != 6 && ft != 7 && ft != 8) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  const ModelDev& m = model->dev;
+  int64_t total = 1;
+  for (int i = 0; i < 5; ++i) total *= m.cd[i];
+  const int64_t total3 = (int64_t)m.cd[0] * m.cd[1] * m.cd[2];
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    std::lock_guard<std::mutex> lock(model->f64_mu);
+    if (!model->d_coeff64) {
+      double *c = nullptr, *c3 = nullptr;
+      cudaError_t e = cudaMalloc(&c, (size_t)total * sizeof(double));
+      if (e == cudaSuccess) e = bsfit::widen_to_f64(model->d_coeff, c, total, st);
+      if (e == cudaSuccess && ft == 8) {
+        e = cudaMalloc(&c3, (size_t)total3 * sizeof(double));
+        if (e == cudaSuccess) e = bsfit::widen_to_f64(model->d_coeff3, c3, total3, st);
+      }
+      // Other threads may use the copies on other streams once published.
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) {
+        cudaFree(c);
+        cudaFree(c3);
+        return cuda_status(e);
+      }
+      model->d_coeff3_64 = c3;
+      model->d_coeff64 = c;
+    }
+  }
+  bsfit::Fit64Args a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = m;
+  a.c = model->d_coeff64;
+  a.c3 = model->d_coeff3_64;
+  a.total = total;
+  a.total3 = total3;
+  a.rois = d_rois;
+  a.var = d_var;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  return cuda_status(bsfit::launch_fit64(a, st));
 }
 
 }  // extern "C"

@@ -90,6 +90,28 @@ struct BatchArgs {
   BatchSeg seg[kMaxBatchSegs];
 };
 
+// FP64 reference-precision fit (fit types 6, 7, 8): double copies of the
+// coefficient tables, float ROIs, double outputs in the column-major layout.
+struct Fit64Args {
+  ModelDev m;
+  const double* c;       // device, the model's table widened to double
+  const double* c3;      // device, fit type 8's 3D table widened to double
+  int64_t total;         // elements of c
+  int64_t total3;        // elements of c3
+  const float* rois;     // device, nfits * s * s
+  const float* var;      // sCMOS variance / gain^2 in the ROI layout, or null
+  int s;
+  int64_t nfits;
+  int iterations;
+  double* P;
+  double* CRLB;
+  double* LL;
+};
+
+cudaError_t launch_fit64(const Fit64Args& a, cudaStream_t stream);
+cudaError_t widen_to_f64(const float* src, double* dst, int64_t n, cudaStream_t stream);
+int fit64_smem_bytes(int mode);
+
 int warp_smem_floats(int mode, int s, bool var = false);
 cudaError_t launch_batch(const BatchArgs& a, int mode, cudaStream_t stream);
 cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream);

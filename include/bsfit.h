@@ -357,6 +357,21 @@ int bsfit_fit_scmos_device(bsfit_model model, const float* d_rois, const float* 
                            float* d_CRLB, float* d_LL, void* stream);
 
 /*
+ * FP64 reference-precision fit (fit types 6, 7, 8): the reference's CPU method
+ * (VC/CPUmleFit_LM/CPUmleFit_LM.cpp:2411-3620 with CPUsplineLib.cpp and
+ * MatInvLib.h) evaluated in double in its own order of operations, so that the
+ * LM takes the decisions of the reference built with float promoted to double.
+ * float ROIs ([nfits][s][s]) and optional sCMOS variance (d_var, same layout,
+ * or NULL); double outputs in bsfit_fit_device's column-major layout. The
+ * model's coefficient table is widened to double on the first call (one
+ * synchronisation of `stream`). Bounded by the device's FP64 rate: a
+ * precision mode next to the FP32 production path, not a replacement.
+ */
+int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_var,
+                         int64_t roi_size, int64_t nfits, int32_t iterations, double* d_P,
+                         double* d_CRLB, double* d_LL, void* stream);
+
+/*
  * Frame -> ROI front end (the step before the fit in the reference's
  * acquisition loop, MultiD_fitter/simplefitter_cspline.m:197-319, with the peak
  * finder MultiD_fitter/shared/maximumfind2.c): photon conversion, filtering,

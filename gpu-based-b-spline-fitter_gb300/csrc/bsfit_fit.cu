@@ -1378,6 +1378,16 @@ __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) fit_kernel(FitArgs
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   float* ws = smem + wib * L.total();
+  if (a.claim) {
+    for (;;) {
+      unsigned long long i = 0;
+      if (lane == 0) i = atomicAdd(a.claim, 1ull);
+      i = __shfl_sync(kFull, i, 0);
+      if ((int64_t)i >= a.nfits) break;
+      fit_and_store<MODE, MULTI, VAR>(a, L, ws, lane, (int64_t)i);
+    }
+    return;
+  }
   const int64_t total_warps = (int64_t)gridDim.x * wpb;
   for (int64_t roi = (int64_t)blockIdx.x * wpb + wib; roi < a.nfits; roi += total_warps)
     fit_and_store<MODE, MULTI, VAR>(a, L, ws, lane, roi);
@@ -1425,6 +1435,7 @@ __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) batch_kernel(const
     fa.n_starts = 0;
     fa.strict = 0;
     fa.var = nullptr;
+    fa.claim = nullptr;
     fit_and_store<MODE, false>(fa, make_layout(MODE, g.s), ws, lane, (int64_t)i);
     if (lane == 0) atomicAdd(&a.done[g.slot], 1ull);
   }
@@ -1615,8 +1626,27 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
   int64_t need = (a.nfits + wpb - 1) / wpb;
   int64_t grid = (int64_t)g_num_sms * blocks_per_sm;
   if (need < grid) grid = need;
-  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(a);
-  return cudaGetLastError();
+  // More ROIs than resident warps: claim them dynamically (iteration counts
+  // vary per ROI, and a fixed share per warp leaves the launch waiting on its
+  // slowest warp). The counter comes from the stream-ordered pool; without it
+  // the fixed schedule runs.
+  FitArgs b = a;
+  unsigned long long* claim = nullptr;
+  if (need > grid) {
+    if (cudaMallocAsync(reinterpret_cast<void**>(&claim), sizeof(*claim), stream) == cudaSuccess) {
+      if (cudaMemsetAsync(claim, 0, sizeof(*claim), stream) == cudaSuccess) {
+        b.claim = claim;
+      } else {
+        cudaFreeAsync(claim, stream);
+        claim = nullptr;
+      }
+    }
+    (void)cudaGetLastError();  // a failed pool allocation leaves the fixed schedule
+  }
+  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(b);
+  e = cudaGetLastError();
+  if (claim) cudaFreeAsync(claim, stream);
+  return e;
 }
 
 }  // namespace bsfit

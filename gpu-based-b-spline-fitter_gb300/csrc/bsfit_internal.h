@@ -57,6 +57,10 @@ struct FitArgs {
   // sCMOS: per-pixel variance / gain^2 in the ROI layout, added to model and
   // data in the likelihood (null: EMCCD)
   const float* var;
+  // Work counter (zeroed device word): warps claim ROIs one at a time, so the
+  // launch ends within one ROI's time of its average warp; null: each warp
+  // takes every (grid warps)-th ROI. Set by launch_fit.
+  unsigned long long* claim;
 };
 
 constexpr int kMaxStarts = 8;

@@ -769,11 +769,12 @@ int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_
     std::lock_guard<std::mutex> lock(model->f64_mu);
     if (!model->d_coeff64) {
       double *c = nullptr, *c3 = nullptr;
-      cudaError_t e = cudaMalloc(&c, (size_t)total * sizeof(double));
-      if (e == cudaSuccess) e = bsfit::widen_to_f64(model->d_coeff, c, total, st);
+      const int D = ft == 6 ? 3 : ft == 7 ? 4 : 5;
+      cudaError_t e = cudaMalloc(&c, (size_t)(D + 1) * total * sizeof(double));
+      if (e == cudaSuccess) e = bsfit::widen_to_f64(model->d_coeff, c, total, D, m.st, st);
       if (e == cudaSuccess && ft == 8) {
-        e = cudaMalloc(&c3, (size_t)total3 * sizeof(double));
-        if (e == cudaSuccess) e = bsfit::widen_to_f64(model->d_coeff3, c3, total3, st);
+        e = cudaMalloc(&c3, (size_t)4 * total3 * sizeof(double));
+        if (e == cudaSuccess) e = bsfit::widen_to_f64(model->d_coeff3, c3, total3, 3, m.st, st);
       }
       // Other threads may use the copies on other streams once published.
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);

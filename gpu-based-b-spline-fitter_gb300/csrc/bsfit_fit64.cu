@@ -23,12 +23,15 @@
 // last bit of log().
 //
 // Layout: one warp per ROI. Lanes evaluate pixels 32 at a time and publish
-// each pixel's (deviance term, 1 - d/m, d/m^2, dudt) in a shared row; the sums
-// are owned one or two entries per lane and accumulated over the rows in pixel
+// each pixel's terms in a shared row (its deviance term, t1 * dudt[l], and
+// (t2 * dudt[l]) * dudt[m], the products the reference adds); the sums are
+// owned one or two entries per lane and accumulated over the rows in pixel
 // order, so every sum has the reference's order. Lane 0 runs the LM control
 // and the small dense solves on shared state. Coefficients are a double copy
-// of the model's table. Throughput is bounded by the FP64 pipe; this is the
-// parity mode, the FP32 kernels are the production path.
+// of the model's table followed by one table per axis of the neighbour
+// differences (-c[i]) + c[i + stride] the derivative terms use (computed once
+// per model, the same double operation). Throughput is bounded by the FP64
+// pipe; this is the parity mode, the FP32 kernels are the production path.
 #include <climits>
 #include <cmath>
 #include <cstdint>
@@ -46,7 +49,7 @@ struct F64Traits<6> {
 };
 template <>
 struct F64Traits<7> {
-  static constexpr int D = 4, NV = 6, WPB = 4;
+  static constexpr int D = 4, NV = 6, WPB = 1;
 };
 template <>
 struct F64Traits<8> {
@@ -78,7 +81,8 @@ struct F64Layout {
   static constexpr int WT = (D + 1) * BB;             // wf, then wd[0..D-1]
   static constexpr int WT3 = (MODE == 8) ? 4 * 64 : 0;  // fit type 8: the 3D tables
   static constexpr int AX = 40;                       // 1-D weights, 4 kinds x 5 axes x 2
-  static constexpr int RW = NV + 3;                   // row: term, t1 / flag, t2 / model, dudt
+  static constexpr int NE = 1 + NV + NV * (NV + 1) / 2;  // sums: deviance, gradient, Hessian
+  static constexpr int RW = NE;                       // row: one term per sum
   static constexpr int ROWS = 32 * RW;
   static constexpr int off_wt = kLMDoubles;
   static constexpr int off_wt3 = off_wt + WT;
@@ -113,13 +117,15 @@ __device__ __forceinline__ double bspline2(double x) {
   return 0.0;
 }
 
+// A model table: values c[0, total) followed by D difference tables,
+// diff(d, i) = (-c[i]) + c[i + stride_d] (0 for a neighbour past the end: only
+// the +1 neighbour of a position exactly on the last knot, whose weight is 0).
 struct Coef {
   const double* c;
   int64_t total;
-  __device__ __forceinline__ double operator()(int64_t i) const {
-    // Only the derivative's +1 neighbour of a position exactly on the last
-    // knot can leave the table (its weight is zero there).
-    return (i < total) ? __ldg(c + i) : 0.0;
+  __device__ __forceinline__ double val(int64_t i) const { return __ldg(c + i); }
+  __device__ __forceinline__ double diff(int d, int64_t i) const {
+    return __ldg(c + (int64_t)(d + 1) * total + i);
   }
 };
 
@@ -203,14 +209,12 @@ __device__ __forceinline__ void pixel_model(const Coef& c, const int* n, const i
       int64_t node = 0;
 #pragma unroll
       for (int a = 0; a < D; ++a) node += ((b >> a) & 1) ? hi[a] : lo[a];
-      const double cv = c(node);
-      const double t = cv * wf[b];
+      const double t = c.val(node) * wf[b];
       s = (b == 0) ? t : s + t;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         double w = W[(1 + d) * BB + B * ni + b];
         int64_t nd = node;
-        double c0 = cv;
         if constexpr (Q5) {
           if (d == 2 && b == 27) {
             // CPUsplineLib.cpp:313 reads delta_dfz[32 * nIndex + 271]; past
@@ -221,10 +225,9 @@ __device__ __forceinline__ void pixel_model(const Coef& c, const int* n, const i
           if (d == 4 && b == 16) {
             // CPUsplineLib.cpp:420-421: the side-1 U node is differenced.
             nd = node - hi[4] + lo[4];
-            c0 = c(nd);
           }
         }
-        const double term = (-c0 + c(nd + st[d])) * w;
+        const double term = c.diff(d, nd) * w;  // (-c[nd] + c[nd + stride]) * w
         sd[d] = (b == 0) ? term : sd[d] + term;
       }
     }
@@ -258,8 +261,9 @@ struct Warp64 {
   double* wt3;
   double* ax;
   double* rows;
-  // Sum entries owned by this lane: kind 0 = deviance / log-likelihood, 1 =
-  // gradient l, 2 = Hessian / Fisher (l, m), m >= l; -1 = none.
+  // Sum entries owned by this lane (entry t = lane + 32 h, also its index in a
+  // row): kind 0 = deviance / log-likelihood, 1 = gradient l, 2 = Hessian /
+  // Fisher (l, m), m >= l; -1 = none.
   int kind[2], el[2], em[2];
 
   __device__ Warp64(double* base, int lane)
@@ -373,7 +377,9 @@ struct Warp64 {
           data += v;
         }
         double* row = rows + lane * RW;
+        int k = 1 + NV;
         if constexpr (FISHER) {
+          // CPUmleFit_LM.cpp:2730-2742
           double term = 0.0, use = 0.0;
           if (model > 0) {
             use = 1.0;
@@ -381,8 +387,12 @@ struct Warp64 {
           }
           row[0] = term;
           row[1] = use;
-          row[2] = model;
+#pragma unroll
+          for (int l = 0; l < NV; ++l)
+#pragma unroll
+            for (int mm = l; mm < NV; ++mm, ++k) row[k] = (dudt[mm] * dudt[l]) / model;
         } else {
+          // CPUmleFit_LM.cpp:2537-2560
           if (dup45) dudt[5] = dudt[4];
           double term;
           if (data > 0) {
@@ -391,32 +401,32 @@ struct Warp64 {
             term = 2.0 * model;
             data = 0.0;
           }
+          const double t1 = 1.0 - data / model;
+          const double t2 = data / (model * model);
           row[0] = term;
-          row[1] = 1.0 - data / model;
-          row[2] = data / (model * model);
-        }
 #pragma unroll
-        for (int l = 0; l < NV; ++l) row[3 + l] = dudt[l];
+          for (int l = 0; l < NV; ++l) row[1 + l] = t1 * dudt[l];
+#pragma unroll
+          for (int l = 0; l < NV; ++l) {
+            const double tl = t2 * dudt[l];
+#pragma unroll
+            for (int mm = l; mm < NV; ++mm, ++k) row[k] = tl * dudt[mm];
+          }
+        }
       }
       __syncwarp();
       const int cnt = (s2 - r0 < 32) ? s2 - r0 : 32;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int kd = kind[h];
-        if (kd < 0) continue;
-        const int l = el[h], mm = em[h];
+        if (kd < 0 || (FISHER && kd == 1)) continue;
+        const int e = lane + 32 * h;
         double a = acc[h];
-        for (int j = 0; j < cnt; ++j) {
-          const double* row = rows + j * RW;
-          if (kd == 0) {
-            if (!FISHER || row[1] != 0.0) a = a + row[0];
-          } else if (kd == 1) {
-            if (!FISHER) a = a + row[1] * row[3 + l];
-          } else if (FISHER) {
-            a = a + (row[3 + mm] * row[3 + l]) / row[2];
-          } else {
-            a = a + (row[2] * row[3 + l]) * row[3 + mm];
-          }
+        if (FISHER && kd == 0) {
+          for (int j = 0; j < cnt; ++j)
+            if (rows[j * RW + 1] != 0.0) a = a + rows[j * RW];
+        } else {
+          for (int j = 0; j < cnt; ++j) a = a + rows[j * RW + e];
         }
         acc[h] = a;
       }
@@ -687,7 +697,7 @@ __device__ void init_state(LMState& st) {
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(32 * F64Traits<MODE>::WPB) fit64_kernel(
+__global__ void __launch_bounds__(32 * F64Traits<MODE>::WPB, 1) fit64_kernel(
     const __grid_constant__ Fit64Args a) {
   using L = F64Layout<MODE>;
   constexpr int NV = L::NV, WPB = F64Traits<MODE>::WPB;
@@ -750,10 +760,23 @@ __global__ void __launch_bounds__(32 * F64Traits<MODE>::WPB) fit64_kernel(
   }
 }
 
-__global__ void widen_kernel(const float* __restrict__ src, double* __restrict__ dst, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    dst[i] = (double)src[i];
+// dst = [c | diff_0 | ... | diff_{D-1}], each `total` long (see Coef).
+struct Strides5 {
+  int64_t st[5];
+};
+
+__global__ void widen_kernel(const float* __restrict__ src, double* __restrict__ dst,
+                             int64_t total, int D, Strides5 st) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double c0 = (double)src[i];
+    dst[i] = c0;
+    for (int d = 0; d < D; ++d) {
+      const int64_t j = i + st.st[d];
+      const double c1 = (j < total) ? (double)src[j] : 0.0;
+      dst[(int64_t)(d + 1) * total + i] = -c0 + c1;
+    }
+  }
 }
 
 template <int MODE>
@@ -789,10 +812,15 @@ int fit64_smem_bytes(int mode) {
   }
 }
 
-cudaError_t widen_to_f64(const float* src, double* dst, int64_t n, cudaStream_t stream) {
-  if (n <= 0) return cudaSuccess;
-  const int64_t blocks = (n + 255) / 256;
-  widen_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(src, dst, n);
+cudaError_t widen_to_f64(const float* src, double* dst, int64_t total, int naxes,
+                         const int64_t* strides, cudaStream_t stream) {
+  if (total <= 0) return cudaSuccess;
+  if (naxes < 0 || naxes > 5) return cudaErrorInvalidValue;
+  Strides5 st{};
+  for (int d = 0; d < naxes; ++d) st.st[d] = strides[d];
+  const int64_t blocks = (total + 255) / 256;
+  widen_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(src, dst, total,
+                                                                              naxes, st);
   return cudaGetLastError();
 }
 

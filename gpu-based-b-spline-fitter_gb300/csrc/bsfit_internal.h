@@ -98,8 +98,10 @@ struct BatchArgs {
 // coefficient tables, float ROIs, double outputs in the column-major layout.
 struct Fit64Args {
   ModelDev m;
-  const double* c;       // device, the model's table widened to double
-  const double* c3;      // device, fit type 8's 3D table widened to double
+  // device: the model's table widened to double, followed by one table per
+  // axis of neighbour differences (-c[i]) + c[i + stride] (widen_to_f64)
+  const double* c;
+  const double* c3;      // the same for fit type 8's 3D table (3 axes)
   int64_t total;         // elements of c
   int64_t total3;        // elements of c3
   const float* rois;     // device, nfits * s * s
@@ -113,7 +115,9 @@ struct Fit64Args {
 };
 
 cudaError_t launch_fit64(const Fit64Args& a, cudaStream_t stream);
-cudaError_t widen_to_f64(const float* src, double* dst, int64_t n, cudaStream_t stream);
+// dst: (1 + naxes) * total doubles, the values then the difference tables.
+cudaError_t widen_to_f64(const float* src, double* dst, int64_t total, int naxes,
+                         const int64_t* strides, cudaStream_t stream);
 int fit64_smem_bytes(int mode);
 
 int warp_smem_floats(int mode, int s, bool var = false);

@@ -104,7 +104,8 @@ def bench_kernel_only(args):
     """Profiling case: warm-up plus timed fits of one workload, nothing else.
     3D (default): one plain launch per size group, or with --batched one
     persistent batched launch per step; --model 5d: fit type 8 on --rois ROIs
-    of 17 px; --model 4pi: the 4Pi fit of --rois ROIs of four 13 px channels."""
+    of 17 px; --model 4pi: the 4Pi fit of --rois ROIs of four 13 px channels;
+    --model 3d64: the FP64 reference-precision kernel on --rois 3D ROIs of 13 px."""
     import torch
     import bsfit
     from bsfit import workloads as W
@@ -120,6 +121,17 @@ def bench_kernel_only(args):
                 m5.fit_torch(r5, w5.iterations, stream=stream)
         stream.synchronize()
         print(json.dumps({"profile_case": True, "model": "5d", "rois": len(w5.rois),
+                          "launches": launches}))
+        return 0
+    if args.model == "3d64":
+        w6 = W.workload_3d(args.rois, s=13, stream=9)
+        m6 = bsfit.Model(6, w6.coeff)
+        r6 = torch.from_numpy(w6.rois).to(dev)
+        with torch.cuda.stream(stream):
+            for _ in range(launches):
+                m6.fit_f64_torch(r6, w6.iterations, stream=stream)
+        stream.synchronize()
+        print(json.dumps({"profile_case": True, "model": "3d64", "rois": len(w6.rois),
                           "launches": launches}))
         return 0
     if args.model == "4pi":
@@ -483,6 +495,27 @@ def bench_gpu(args):
             b4.record(stream)
         stream.synchronize()
         fits_4pi = w4.n_fits / (a4.elapsed_time(b4) / 2 * 1e-3)
+    # FP64 reference-precision kernel (bit-identical to the FP64 oracle) on
+    # 3D 13 px ROIs of the step's workload.
+    fp64_fig = None
+    if not args.no_fp64:
+        g13 = next(g for g in groups if g.roi_size == 13)
+        n64 = min(args.rois_fp64, len(g13.rois))
+        r64 = d_rois[groups.index(g13)][:n64]
+        m64 = models[id(g13.coeff)]
+        with torch.cuda.stream(stream):
+            m64.fit_f64_torch(r64, g13.iterations, stream=stream)
+            a6, b6 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a6.record(stream)
+            for _ in range(2):
+                m64.fit_f64_torch(r64, g13.iterations, stream=stream)
+            b6.record(stream)
+        stream.synchronize()
+        fp64_fig = {"3d_13px_fits_per_s": n64 / (a6.elapsed_time(b6) / 2 * 1e-3),
+                    "workload": f"{n64} ROIs 13x13 of the step, fit type 6, "
+                                f"{g13.iterations}-iteration cap",
+                    "kernel": "fit64_kernel<6>: the reference method in double, bit-identical "
+                              "to the FP64 oracle"}
     # Coefficient builder (bsarray, degree 3) on the 5D grid: GPU kernel
     # against the numpy restatement on the host.
     prefilter_fig = None
@@ -548,6 +581,7 @@ def bench_gpu(args):
                        "5d_workload": f"{args.rois_5d} ROIs 17x17, fit type 8, 60 iterations",
                        "4pi_13px": fits_4pi,
                        "4pi_workload": f"{args.rois_4pi} ROIs of 4 channels 13x13, 100 iterations"},
+        "reference_precision": fp64_fig,
         "prefilter": prefilter_fig,
         "frontend": frontend_fig,
         "serving": serving,
@@ -568,13 +602,16 @@ def main():
                     help="profiling case: only the fit launches of --rois ROIs of --sizes")
     ap.add_argument("--rois", type=int, default=N_ROIS)
     ap.add_argument("--batched", action="store_true", help="kernel-only: the batched form")
-    ap.add_argument("--model", default="3d", choices=["3d", "5d", "4pi"], help="kernel-only: model")
+    ap.add_argument("--model", default="3d", choices=["3d", "5d", "4pi", "3d64"],
+                    help="kernel-only: model")
     ap.add_argument("--sizes", type=int, nargs="+", default=list(SIZES))
     ap.add_argument("--rois-5d", type=int, default=50000, help="ROIs of the 5D 17 px figure")
     ap.add_argument("--no-5d", action="store_true")
     ap.add_argument("--rois-4pi", type=int, default=100000, help="ROIs of the 4Pi figure")
     ap.add_argument("--no-4pi", action="store_true")
     ap.add_argument("--no-prefilter", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--rois-fp64", type=int, default=100000, help="ROIs of the FP64 figure")
     ap.add_argument("--no-frontend", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-frames", type=int, default=80)

@@ -31,14 +31,16 @@ def _dims(a):
 
 
 def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, silent=1,
-                        initP=None, coeff3=None, out=None):
+                        initP=None, coeff3=None, out=None, precision="f32"):
     """Drop-in for the reference mex (fit types 6, 7, 8); raises BsfitError.
 
     Returns (P, CRLB, LL) shaped (N, NV + 1), (N, NV), (N,): views of the C
     ABI's column-major outputs (no copy). out=(P, CRLB, LL) passes caller-owned
-    float32 buffers in the C ABI's layout ((NV + 1, N), (NV, N), (N,)), which
-    are filled and returned as the same views, as a host application calling
-    the C ABI directly would reuse its buffers."""
+    buffers in the C ABI's layout ((NV + 1, N), (NV, N), (N,)), which are
+    filled and returned as the same views, as a host application calling the C
+    ABI directly would reuse its buffers. precision="f64" runs the FP64
+    reference-precision kernel (bsfit_GPUmleFit_LM_multiD_f64) and returns
+    float64 results, those of the reference method computed in double."""
     lib = _native.lib()
     im = _f32(imstack)
     if im.ndim == 2:
@@ -52,22 +54,27 @@ def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, s
     c3 = _f32(coeff3) if coeff3 is not None else None
     ip = _f32(np.atleast_1d(initP)) if initP is not None else None
     vm = _f32(np.atleast_1d(varmap)) if varmap is not None else None
+    if precision not in ("f32", "f64"):
+        raise ValueError("precision must be 'f32' or 'f64'")
+    dt = np.float32 if precision == "f32" else np.float64
     if out is None:
-        P = np.empty((max(nv, 1) + 1, n), np.float32)
-        C = np.empty((max(nv, 1), n), np.float32)
-        L = np.empty(n, np.float32)
+        P = np.empty((max(nv, 1) + 1, n), dt)
+        C = np.empty((max(nv, 1), n), dt)
+        L = np.empty(n, dt)
     else:
         P, C, L = out
         assert P.shape == (nv + 1, n) and C.shape == (nv, n) and L.shape == (n,)
-        assert all(x.dtype == np.float32 and x.flags.c_contiguous for x in (P, C, L))
+        assert all(x.dtype == dt and x.flags.c_contiguous for x in (P, C, L))
     ptr = lambda a: a.ctypes.data_as(_fp) if a is not None else None  # noqa: E731
-    st = lib.bsfit_GPUmleFit_LM_multiD(
+    optr = (lambda a: a.ctypes.data_as(_fp)) if precision == "f32" else (lambda a: a.ctypes.data)
+    fn = lib.bsfit_GPUmleFit_LM_multiD if precision == "f32" else lib.bsfit_GPUmleFit_LM_multiD_f64
+    st = fn(
         ptr(im), s1, s2, n, fittype, int(iterations),
         ptr(c), c.ndim if c is not None else 0, _dims(c) if c is not None else None,
         ptr(vm), vm.size if vm is not None else 0, int(silent),
         ptr(ip), ip.size if ip is not None else 0,
         ptr(c3), c3.ndim if c3 is not None else 0, _dims(c3) if c3 is not None else None,
-        ptr(P), ptr(C), ptr(L))
+        optr(P), optr(C), optr(L))
     check(st, "GPUmleFit_LM_multiD")
     return P.T, C.T, L
 

@@ -22,6 +22,10 @@ SIGNATURES = {
         _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
         _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int64,
         _fp, ctypes.c_int32, _i64p, _fp, _fp, _fp]),
+    "bsfit_GPUmleFit_LM_multiD_f64": (ctypes.c_int, [
+        _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+        _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int64,
+        _fp, ctypes.c_int32, _i64p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "bsfit_model_create": (ctypes.c_int, [
         ctypes.c_int32, _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int32, _i64p, _fp,
         ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),

@@ -158,6 +158,21 @@ CallStreams* call_streams() {
   return &cs;
 }
 
+// Argument checks of the synchronous drop-in calls, in the reference's order
+// (mex :247-263), then the device count.
+int call_checks(const float* imstack, int64_t roi_size, int64_t roi_size2, int64_t nfits,
+                int fittype, bool outputs) {
+  if (!imstack) return BSFIT_E_WRONG_DATA_TYPE;
+  if (roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (roi_size2 != roi_size) return BSFIT_E_SUBREGION_SHAPE;
+  if (roi_size < 1 || nfits < 0) return BSFIT_E_INVALID;
+  if (num_params(fittype) == 0) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (!outputs) return BSFIT_E_INVALID;
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count < 1) return BSFIT_E_NO_DEVICE;
+  return BSFIT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -385,22 +400,15 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
                               float* CRLB, float* LL) {
   (void)varmap;
   (void)varmap_numel;  // ignored for fit types 6-8, as in the reference
-  // Argument checks in the reference's order (mex :247-263).
-  if (!imstack) return BSFIT_E_WRONG_DATA_TYPE;
-  if (roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
-  if (roi_size2 != roi_size) return BSFIT_E_SUBREGION_SHAPE;
-  if (roi_size < 1 || nfits < 0) return BSFIT_E_INVALID;
-  if (num_params(fittype) == 0) return BSFIT_E_UNSUPPORTED_FITTYPE;
-  if (!P || !CRLB || !LL) return BSFIT_E_INVALID;
-  int dev_count = 0;
-  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count < 1) return BSFIT_E_NO_DEVICE;
+  int st = call_checks(imstack, roi_size, roi_size2, nfits, fittype, P && CRLB && LL);
+  if (st) return st;
   const int nv = num_params(fittype);
   if (!silent) {
     std::printf("subregion size: %lld fittype: %d\n", (long long)roi_size, fittype);
     std::printf("Number of fits: %lld no padding\n", (long long)nfits);
   }
-  int st = check_model_args(fittype, coeff, coeff_ndim, coeff_dims, coeff3, coeff3_ndim,
-                            coeff3_dims, init_p, init_p_numel);
+  st = check_model_args(fittype, coeff, coeff_ndim, coeff_dims, coeff3, coeff3_ndim,
+                        coeff3_dims, init_p, init_p_numel);
   if (st) return st;
   if (nfits == 0) return BSFIT_OK;
   // Memory check (mex :409-456): refuse work above 95% of free memory.
@@ -803,6 +811,68 @@ int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_
   a.CRLB = d_CRLB;
   a.LL = d_LL;
   return cuda_status(bsfit::launch_fit64(a, st));
+}
+
+// The drop-in call with double results from the FP64 reference-precision
+// kernel: same arguments and checks as bsfit_GPUmleFit_LM_multiD (varmap
+// ignored likewise), double outputs in the same column-major layout.
+int bsfit_GPUmleFit_LM_multiD_f64(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                                  int64_t nfits, int32_t fittype, int32_t iterations,
+                                  const float* coeff, int32_t coeff_ndim,
+                                  const int64_t* coeff_dims, const float* varmap,
+                                  int64_t varmap_numel, int32_t silent, const float* init_p,
+                                  int64_t init_p_numel, const float* coeff3, int32_t coeff3_ndim,
+                                  const int64_t* coeff3_dims, double* P, double* CRLB,
+                                  double* LL) {
+  (void)varmap;
+  (void)varmap_numel;
+  int st = call_checks(imstack, roi_size, roi_size2, nfits, fittype, P && CRLB && LL);
+  if (st) return st;
+  const int nv = num_params(fittype);
+  if (!silent) {
+    std::printf("subregion size: %lld fittype: %d\n", (long long)roi_size, fittype);
+    std::printf("Number of fits: %lld no padding\n", (long long)nfits);
+  }
+  bsfit_model model = nullptr;
+  st = bsfit_model_create(fittype, coeff, coeff_ndim, coeff_dims, coeff3, coeff3_ndim,
+                          coeff3_dims, init_p, init_p_numel, &model);
+  if (st) return st;
+  if (nfits == 0) return bsfit_model_release(model);
+  CallStreams* cs = call_streams();
+  if (!cs) {
+    bsfit_model_release(model);
+    return BSFIT_E_CUDA;
+  }
+  cudaStream_t cst = cs->comp[0];
+  const size_t s2 = (size_t)roi_size * roi_size;
+  const size_t in_bytes = (size_t)nfits * s2 * sizeof(float);
+  const size_t nout = (size_t)nfits * (2 * nv + 2);
+  float* d_rois = nullptr;
+  double* d_out = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_rois, in_bytes, cst);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_out, nout * sizeof(double), cst);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rois, imstack, in_bytes, cudaMemcpyHostToDevice, cst);
+  int rc = BSFIT_OK;
+  double* dP = d_out;
+  double* dC = d_out + (size_t)nfits * (nv + 1);
+  double* dL = dC + (size_t)nfits * nv;
+  if (e == cudaSuccess)
+    rc = bsfit_fit_f64_device(model, d_rois, nullptr, roi_size, nfits, iterations, dP, dC, dL,
+                              cst);
+  if (e == cudaSuccess && rc == BSFIT_OK)
+    e = cudaMemcpyAsync(P, dP, (size_t)nfits * (nv + 1) * sizeof(double), cudaMemcpyDeviceToHost,
+                        cst);
+  if (e == cudaSuccess && rc == BSFIT_OK)
+    e = cudaMemcpyAsync(CRLB, dC, (size_t)nfits * nv * sizeof(double), cudaMemcpyDeviceToHost, cst);
+  if (e == cudaSuccess && rc == BSFIT_OK)
+    e = cudaMemcpyAsync(LL, dL, (size_t)nfits * sizeof(double), cudaMemcpyDeviceToHost, cst);
+  if (d_rois) cudaFreeAsync(d_rois, cst);
+  if (d_out) cudaFreeAsync(d_out, cst);
+  cudaError_t e2 = cudaStreamSynchronize(cst);
+  bsfit_model_release(model);
+  if (rc != BSFIT_OK) return rc;
+  if (e == cudaSuccess) e = e2;
+  return cuda_status(e);
 }
 
 }  // extern "C"

@@ -372,6 +372,21 @@ int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_
                          double* d_CRLB, double* d_LL, void* stream);
 
 /*
+ * The synchronous drop-in call (bsfit_GPUmleFit_LM_multiD: same arguments,
+ * checks and status codes, varmap likewise ignored) with double outputs from
+ * the FP64 reference-precision kernel: the reference's results as its CPU
+ * method computes them in double.
+ */
+int bsfit_GPUmleFit_LM_multiD_f64(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                                  int64_t nfits, int32_t fittype, int32_t iterations,
+                                  const float* coeff, int32_t coeff_ndim,
+                                  const int64_t* coeff_dims, const float* varmap,
+                                  int64_t varmap_numel, int32_t silent, const float* init_p,
+                                  int64_t init_p_numel, const float* coeff3, int32_t coeff3_ndim,
+                                  const int64_t* coeff3_dims, double* P, double* CRLB,
+                                  double* LL);
+
+/*
  * Frame -> ROI front end (the step before the fit in the reference's
  * acquisition loop, MultiD_fitter/simplefitter_cspline.m:197-319, with the peak
  * finder MultiD_fitter/shared/maximumfind2.c): photon conversion, filtering,

@@ -102,3 +102,45 @@ def test_f64_rejects(bsfit_mod):
     assert lib.bsfit_fit_f64_device(m._h, r.data_ptr(), None, 52, 4, 10, p, p, p, None) == 3
     assert lib.bsfit_fit_f64_device(m._h, None, None, 13, 4, 10, p, p, p, None) == 11
     assert lib.bsfit_fit_f64_device(m._h, r.data_ptr(), None, 13, 0, 10, p, p, p, None) == 0
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_f64_dropin_host_call(bsfit_mod, case):
+    """The host drop-in with precision="f64" (bsfit_GPUmleFit_LM_multiD_f64)
+    returns the device entry point's results bit for bit; against the
+    reference's own FP64 build (fixture) the parameters of every finite ROI are
+    bit-identical up to log()-rounding flips (at most one ROI per case)."""
+    d = np.load(os.path.join(GOLDEN, case + ".npz"))
+    ft = int(d["fittype"])
+    nv = NV[ft]
+    kw = {}
+    if "init_p" in d:
+        kw["initP"] = d["init_p"]
+    if "coeff3" in d:
+        kw["coeff3"] = d["coeff3"]
+    P, C, L = bsfit_mod.GPUmleFit_LM_multiD(d["rois"], ft, int(d["iterations"]), d["coeff"],
+                                            precision="f64", **kw)
+    assert P.dtype == np.float64 and C.dtype == np.float64 and L.dtype == np.float64
+    Pd, Cd, Ld = _fit64(bsfit_mod, ft, d["rois"], int(d["iterations"]), d["coeff"],
+                        init_p=d["init_p"] if "init_p" in d else None,
+                        coeff3=d["coeff3"] if "coeff3" in d else None)
+    assert np.array_equal(P, Pd, equal_nan=True)
+    assert np.array_equal(C, Cd, equal_nan=True)
+    assert np.array_equal(L, Ld, equal_nan=True)
+    R = d["f64_P"]
+    same = np.all((P == R) | (np.isnan(P) & np.isnan(R)), axis=1)
+    print(f"{case}: {same.mean():.4f} of ROIs bit-identical to the reference's FP64 build")
+    assert (~same).sum() <= 1, (case, np.where(~same)[0])
+
+
+def test_f64_dropin_rejects(bsfit_mod):
+    from bsfit import BsfitError
+    from bsfit import workloads as W
+    w3 = W.workload_3d(4, s=13, stream=966)
+    with pytest.raises(BsfitError):
+        bsfit_mod.GPUmleFit_LM_multiD(np.zeros((2, 52, 52), np.float32), 6, 10, w3.coeff,
+                                      precision="f64")
+    with pytest.raises(BsfitError):
+        bsfit_mod.GPUmleFit_LM_multiD(w3.rois, 3, 10, w3.coeff, precision="f64")
+    with pytest.raises(ValueError):
+        bsfit_mod.GPUmleFit_LM_multiD(w3.rois, 6, 10, w3.coeff, precision="f16")

@@ -39,6 +39,19 @@ SIZES = (11, 13, 17)
 ITERATIONS = 30
 
 
+def aggregate_ranks(ms, n_local, world, device=None):
+    """Whole-job figure of a replicated step: every rank fits its own copy of
+    the workload, so the job processes n_local * world fits in the slowest
+    rank's time (max over ranks). Returns (max ms, fits/s)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, n_local * world / (ms * 1e-3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -403,12 +416,7 @@ def bench_gpu(args):
         stream.synchronize()
     torch.cuda.synchronize()
     barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = t.item()
-    value = n_step * world / (ms * 1e-3)
+    ms, value = aggregate_ranks(ev0.elapsed_time(ev1) / args.steps, n_step, world, dev)
 
     # Per-size kernel times of the plain form (one launch per size group, events
     # on the launch stream) and the roofline of the fitter kernel.
@@ -450,8 +458,8 @@ def bench_gpu(args):
             bsfit.GPUmleFit_LM_multiD(p, 6, g.iterations, g.coeff, out=o)
     torch.cuda.synchronize()
     barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e_value = n_step * world / e2e_s
+    _, e2e_value = aggregate_ranks((time.perf_counter() - t0) / e2e_steps * 1e3, n_step, world,
+                                   dev)
 
     # The metric's per-model figures: 3D 13 px from the per-size timing above,
     # 5D 17 px (fit type 8, 60 iterations) on its own synthetic workload.

@@ -227,8 +227,55 @@ def bench_reference(args):
             "cpu_baseline": {"value": v, "unit": "fits/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_ref_gpu:
+        line["reference_gpu_kernel"] = bench_reference_gpu(groups)
     print(json.dumps(line))
     return 0
+
+
+def bench_reference_gpu(groups):
+    """Informational: the reference's own CUDA kernels (one thread per ROI, as
+    its mex launches them) on this GPU, device-resident ROIs, CUDA events; the
+    3D 13 px group of the step, the 4D 13 px and 5D 17 px synthetic models."""
+    try:
+        import torch
+        from oracle import ref_gpu
+        if not (torch.cuda.is_available() and ref_gpu.available()):
+            return {"unavailable": "no GPU or the reference PTX is not built"}
+        from bsfit import workloads as W
+        dev = torch.device("cuda", 0)
+        r = ref_gpu.RefGPU()
+        stream = torch.cuda.Stream(dev)
+        out = {}
+        g13 = next(g for g in groups if g.roi_size == 13)
+        w4 = W.workload_4d(20000, sizes=(13,), stream=402)[0]
+        w5 = W.workload_5d(2000, s=17, stream=403)
+        cases = [("3d_13px", 6, g13.rois[:100000], g13), ("4d_13px", 7, w4.rois, w4),
+                 ("5d_17px", 8, w5.rois, w5)]
+        for key, ft, rois, wl in cases:
+            d_r = torch.from_numpy(np.ascontiguousarray(rois)).to(dev)
+            d_c = r.padded_table(wl.coeff, dev)
+            d_c3 = r.padded_table(wl.coeff3, dev) if ft == 8 else None
+            ip = None
+            if ft in (7, 8):
+                ip = torch.from_numpy(np.asarray(wl.init_p, np.float32)).to(dev)
+            dims = list(reversed(wl.coeff.shape))
+            with torch.cuda.stream(stream):
+                o = r.fit(ft, d_r, wl.iterations, d_c, dims, d_c3, ip, stream=stream)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for _ in range(2):
+                    r.fit(ft, d_r, wl.iterations, d_c, dims, d_c3, ip, stream=stream, out=o)
+                b.record(stream)
+            stream.synchronize()
+            out[key] = len(rois) / (a.elapsed_time(b) / 2 * 1e-3)
+        out["workloads"] = ("3D: 100000 ROIs of the step's 13 px group, 30 iterations; 4D: "
+                            "20000 ROIs 13 px, 60 iterations; 5D: 2000 ROIs 17 px, 60 iterations")
+        out["unit"] = "fits/s"
+        out["kernels"] = "GPUmleFit_LM_EMCCD.cu kernel_bsplineMLEFit_*, 64 threads per block"
+        return out
+    except Exception as e:  # informational figure: report why it is missing
+        return {"unavailable": f"{type(e).__name__}: {e}"[:300]}
 
 
 def bench_serving(args, dev, seed=11):
@@ -619,6 +666,8 @@ def main():
     ap.add_argument("--no-4pi", action="store_true")
     ap.add_argument("--no-prefilter", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="reference arm: skip the reference GPU kernel figure")
     ap.add_argument("--rois-fp64", type=int, default=100000, help="ROIs of the FP64 figure")
     ap.add_argument("--no-frontend", action="store_true")
     ap.add_argument("--no-serve", action="store_true")

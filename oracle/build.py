@@ -33,8 +33,9 @@ def build_reference(force=False):
                        "CPUmleFit_LM", "CPUmleFit_LM.cpp")
     if not os.path.exists(src):
         return None
-    out = os.path.join(REF_DIR, "libref_f32.so")
-    if not force and os.path.exists(out) and os.path.exists(os.path.join(REF_DIR, "libref_f64.so")):
+    done = all(os.path.exists(os.path.join(REF_DIR, f))
+               for f in ("libref_f32.so", "libref_f64.so", "ref_emccd.ptx"))
+    if not force and done:
         return REF_DIR
     subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True)
     return REF_DIR

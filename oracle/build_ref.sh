@@ -4,6 +4,7 @@
 #   oracle/_ref/libref_f32.so  FP32, as shipped
 #   oracle/_ref/libref_f64.so  the same sources with float promoted to double
 #   oracle/_ref/libref_maxfind.so  the peak finder MultiD_fitter/shared/maximumfind2.c
+#   oracle/_ref/ref_emccd.ptx  the reference's CUDA fitter kernels (PTX, sm_103a)
 # Only the three fitter sources are compiled (not erf.cpp, which the reference's
 # own project does not build, nor the mex driver, which needs MATLAB).
 # -fno-stack-protector: the 8-parameter solver kernel_luEvaluate5D declares
@@ -48,4 +49,14 @@ if [ -f "$PEAK" ]; then
   "$CC" -shared -Wl,--no-undefined -o "$OUT/libref_maxfind.so" "$OUT/maximumfind2.o" "$OUT/mex_stubs.o"
   rm -f "$OUT/maximumfind2.o" "$OUT/mex_stubs.o"
 fi
-echo "built $OUT/libref_f32.so $OUT/libref_f64.so $OUT/libref_maxfind.so"
+# The reference's own CUDA kernels (VC/GPUmleFit_LM/GPUmleFit_LM_EMCCD.cu with
+# the headers of VC/Lib), compiled as the reference's project does (one
+# translation unit) but to PTX for compute_103a, loaded through the driver API
+# by oracle/ref_gpu.py: the reference GPU kernel timed on the same device.
+GPU="$REF/MultiD_bspline/visual code/GPUmleFit_LM"
+if [ -f "$GPU/GPUmleFit_LM_EMCCD.cu" ] && command -v "${NVCC:-nvcc}" > /dev/null; then
+  "${NVCC:-nvcc}" -arch=compute_103a -ptx -O3 -w -I "$HERE/ref_shim_mex" \
+    -I "$REF/MultiD_bspline/visual code/Lib" -I "$GPU" "$GPU/GPUmleFit_LM_EMCCD.cu" \
+    -o "$OUT/ref_emccd.ptx"
+fi
+echo "built $OUT/libref_f32.so $OUT/libref_f64.so $OUT/libref_maxfind.so $OUT/ref_emccd.ptx"

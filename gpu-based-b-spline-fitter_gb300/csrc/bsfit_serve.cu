@@ -59,7 +59,6 @@ class Arena {
         int64_t off = it->first, len = it->second;
         free_.erase(it);
         if (len > bytes) free_[off + bytes] = len - bytes;
-        used_ += bytes;
         return off;
       }
     }
@@ -67,7 +66,6 @@ class Arena {
   }
   void release(int64_t off, int64_t bytes) {
     bytes = (bytes + 255) / 256 * 256;
-    used_ -= bytes;
     auto it = free_.emplace(off, bytes).first;
     auto nx = std::next(it);
     if (nx != free_.end() && it->first + it->second == nx->first) {
@@ -83,10 +81,9 @@ class Arena {
     }
   }
   int64_t size() const { return size_; }
-  int64_t used() const { return used_; }
 
  private:
-  int64_t size_ = 0, used_ = 0;
+  int64_t size_ = 0;
   std::map<int64_t, int64_t> free_;
 };
 

@@ -83,7 +83,10 @@ def test_f64_scmos_parity(bsfit_mod, oracle):
     R, RC, RL = oracle.fit(noisy, 7, wl.iterations, wl.coeff, init_p=wl.init_p, precision="f64",
                            threads=os.cpu_count() or 1, var=var)
     ok = tol_pass(P, C, R, RC, 6)
-    assert ok.mean() >= 0.97, ok.mean()
+    same = np.all(P == R, axis=1)
+    print(f"sCMOS fit type 7: {ok.mean():.4f} within tolerance, {same.mean():.4f} bit-identical")
+    assert ok.mean() >= 0.99, ok.mean()
+    assert same.mean() >= 0.99, same.mean()
 
 
 def test_f64_rejects(bsfit_mod):

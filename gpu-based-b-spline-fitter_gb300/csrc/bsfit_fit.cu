@@ -34,6 +34,7 @@
 // derivative difference) is never read.
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 
 #include "bsfit_device.cuh"
 #include "bsfit_internal.h"
@@ -1441,6 +1442,76 @@ __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) batch_kernel(const
   }
 }
 
+// Launch shape of a fitter kernel for a per-warp shared-memory size: the warps
+// per block among 4, 2, 1 that keep the most warps resident per SM, with the
+// blocks per SM and the SM count. Computed once per (kernel, size, device) and
+// cached; the kernel's dynamic shared-memory limit is raised to the device's
+// opt-in maximum on its first use, so launches of any size need no further
+// attribute call.
+namespace {
+struct LaunchChoice {
+  const void* kern;
+  int per_warp, dev, wpb, bps, sms;
+};
+std::mutex g_choice_mu;
+constexpr int kMaxChoices = 128;
+LaunchChoice g_choices[kMaxChoices];
+int g_nchoices = 0;
+struct RaisedKernel {
+  const void* kern;
+  int dev;
+};
+RaisedKernel g_raised[64];
+int g_nraised = 0;
+}  // namespace
+
+cudaError_t pick_launch(const void* kern, int per_warp, int* wpb, int* bps, int* sms) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_choice_mu);
+  for (int i = 0; i < g_nchoices; ++i) {
+    const LaunchChoice& c = g_choices[i];
+    if (c.kern == kern && c.per_warp == per_warp && c.dev == dev) {
+      *wpb = c.wpb;
+      *bps = c.bps;
+      *sms = c.sms;
+      return cudaSuccess;
+    }
+  }
+  int optin = 0, nsm = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  bool raised = false;
+  for (int i = 0; i < g_nraised; ++i) raised |= (g_raised[i].kern == kern && g_raised[i].dev == dev);
+  if (!raised) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e != cudaSuccess) return e;
+    if (g_nraised < 64) g_raised[g_nraised++] = RaisedKernel{kern, dev};
+  }
+  int best = -1, bw = 4, bb = 0;
+  for (int cand = 4; cand >= 1; cand >>= 1) {
+    const int sm = per_warp * cand;
+    if (sm > optin) continue;
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * cand, sm) != cudaSuccess) continue;
+    if (b * cand > best) {
+      best = b * cand;
+      bw = cand;
+      bb = b;
+    }
+  }
+  if (best <= 0) return cudaErrorInvalidConfiguration;
+  const LaunchChoice c{kern, per_warp, dev, bw, bb, nsm};
+  if (g_nchoices < kMaxChoices) g_choices[g_nchoices++] = c;
+  else g_choices[(per_warp + dev) % kMaxChoices] = c;
+  *wpb = bw;
+  *bps = bb;
+  *sms = nsm;
+  return cudaSuccess;
+}
+
 cudaError_t launch_batch(const BatchArgs& a, int mode, cudaStream_t stream) {
   if (a.nseg <= 0) return cudaSuccess;
   const int per_warp = warp_smem_floats(mode, a.s_max) * 4;
@@ -1449,27 +1520,10 @@ cudaError_t launch_batch(const BatchArgs& a, int mode, cudaStream_t stream) {
   else if (mode == 7) kern = batch_kernel<7>;
   else if (mode == 8) kern = batch_kernel<8>;
   else return cudaErrorInvalidValue;
-  int wpb = 4, blocks_per_sm = 0, best = -1;
-  for (int cand = 4; cand >= 1; cand >>= 1) {
-    const int sm = per_warp * cand;
-    if (sm > 220 * 1024) continue;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
-      continue;
-    int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * cand, sm) != cudaSuccess) continue;
-    if (b * cand > best) {
-      best = b * cand;
-      wpb = cand;
-      blocks_per_sm = b;
-    }
-  }
-  if (best <= 0) return cudaErrorInvalidConfiguration;
-  const int smem = per_warp * wpb;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int wpb = 4, blocks_per_sm = 0, sms = 0;
+  cudaError_t e = pick_launch((const void*)kern, per_warp, &wpb, &blocks_per_sm, &sms);
   if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int smem = per_warp * wpb;
   int64_t total = 0;
   for (int i = 0; i < a.nseg; ++i) total += a.seg[i].n;
   int64_t grid = (int64_t)sms * blocks_per_sm;
@@ -1583,15 +1637,8 @@ cudaError_t measure_fp32_peak(double* tflops) {
 
 // ---------------------------------------------------------------------------
 
-static int g_num_sms = 0;
-
 cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
   if (a.nfits <= 0) return cudaSuccess;
-  if (g_num_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-  }
   const int mode = a.m.fittype;
   const bool var = a.var != nullptr;
   const int per_warp = warp_smem_floats(mode, a.s, var) * 4;
@@ -1605,26 +1652,12 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
   else return cudaErrorInvalidValue;
   // Warps per block: the choice among 4, 2, 1 that keeps the most warps
   // resident per SM (shared memory per warp grows with s and the model).
-  int wpb = 4, blocks_per_sm = 0, best = -1;
-  for (int cand = 4; cand >= 1; cand >>= 1) {
-    const int sm = per_warp * cand;
-    if (sm > 220 * 1024) continue;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
-      continue;
-    int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * cand, sm) != cudaSuccess) continue;
-    if (b * cand > best) {
-      best = b * cand;
-      wpb = cand;
-      blocks_per_sm = b;
-    }
-  }
-  if (best <= 0) return cudaErrorInvalidConfiguration;
-  const int smem = per_warp * wpb;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int wpb = 4, blocks_per_sm = 0, sms = 0;
+  cudaError_t e = pick_launch((const void*)kern, per_warp, &wpb, &blocks_per_sm, &sms);
   if (e != cudaSuccess) return e;
+  const int smem = per_warp * wpb;
   int64_t need = (a.nfits + wpb - 1) / wpb;
-  int64_t grid = (int64_t)g_num_sms * blocks_per_sm;
+  int64_t grid = (int64_t)sms * blocks_per_sm;
   if (need < grid) grid = need;
   // More ROIs than resident warps: claim them dynamically (iteration counts
   // vary per ROI, and a fixed share per warp leaves the launch waiting on its

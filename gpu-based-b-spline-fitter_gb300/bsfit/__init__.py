@@ -346,9 +346,12 @@ class Batch:
     """Batched fit of ROI segments (mixed ROI sizes and models) with one
     persistent launch per fit type. Each entry: (model, rois_cuda_tensor,
     iterations). Outputs are allocated once and reused across calls; the work
-    queue lives in a small device scratch buffer owned by the batch."""
+    queue lives in a small device scratch buffer owned by the batch.
+    starts (fit types 7, 8): one sequence of initP vectors per entry, fitted
+    from each inside the launch with the best log-likelihood kept (strict: the
+    4D GUI's "> 1e-4" rule instead of ">= 1e-4")."""
 
-    def __init__(self, entries, device=None):
+    def __init__(self, entries, device=None, starts=None, strict=False):
         import torch
         if not 0 < len(entries) <= 48:
             raise ValueError("a batch holds 1 to 48 segments")
@@ -369,15 +372,37 @@ class Batch:
             segs[k].iterations = int(it)
             segs[k].d_P, segs[k].d_CRLB, segs[k].d_LL = P.data_ptr(), C.data_ptr(), L.data_ptr()
         self._segs = segs
+        self._starts = None
+        if starts is not None:
+            if len(starts) != len(self.entries):
+                raise ValueError("one starts sequence per entry")
+            st = (_native.Starts * len(self.entries))()
+            for k, sv in enumerate(starts):
+                a = np.atleast_2d(np.asarray(sv, np.float32))
+                if not 1 <= a.shape[0] <= 8 or a.shape[1] > 4:
+                    raise ValueError("1 to 8 starts of at most 4 values per entry")
+                st[k].n_starts = a.shape[0]
+                st[k].strict = int(bool(strict))
+                for i in range(a.shape[0]):
+                    for j in range(a.shape[1]):
+                        st[k].initp[i][j] = float(a[i, j])
+            self._starts = st
         nb = _native.lib().bsfit_batch_scratch_bytes(len(self.entries))
         self.scratch = torch.zeros((max(nb, 256) // 8,), dtype=torch.int64, device=dev)
 
     def run(self, stream=None):
         import torch
         st = stream if stream is not None else torch.cuda.current_stream(self.scratch.device)
-        check(_native.lib().bsfit_batch_fit_device(
-            np.ctypeslib.ctypes.cast(self._segs, np.ctypeslib.ctypes.c_void_p), len(self.entries),
-            self.scratch.data_ptr(), self.scratch.numel() * 8, st.cuda_stream), "bsfit_batch_fit_device")
+        ct = np.ctypeslib.ctypes
+        if self._starts is None:
+            check(_native.lib().bsfit_batch_fit_device(
+                ct.cast(self._segs, ct.c_void_p), len(self.entries), self.scratch.data_ptr(),
+                self.scratch.numel() * 8, st.cuda_stream), "bsfit_batch_fit_device")
+        else:
+            check(_native.lib().bsfit_batch_fit_multistart_device(
+                ct.cast(self._segs, ct.c_void_p), ct.cast(self._starts, ct.c_void_p),
+                len(self.entries), self.scratch.data_ptr(), self.scratch.numel() * 8,
+                st.cuda_stream), "bsfit_batch_fit_multistart_device")
         return self.outputs
 
     def counters(self):

@@ -41,6 +41,9 @@ SIGNATURES = {
     "bsfit_batch_fit_device": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "bsfit_batch_fit_device_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "bsfit_batch_fit_multistart_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
+        ctypes.c_void_p]),
     "bsfit_model_fittype": (ctypes.c_int32, [ctypes.c_void_p]),
     "bsfit_server_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64,
                                            ctypes.POINTER(ctypes.c_void_p)]),
@@ -132,6 +135,12 @@ class Segment(ctypes.Structure):
                 ("roi_size", ctypes.c_int64), ("nfits", ctypes.c_int64),
                 ("iterations", ctypes.c_int32), ("d_P", ctypes.c_void_p),
                 ("d_CRLB", ctypes.c_void_p), ("d_LL", ctypes.c_void_p)]
+
+
+class Starts(ctypes.Structure):
+    """bsfit_starts (include/bsfit.h)."""
+    _fields_ = [("n_starts", ctypes.c_int32), ("strict", ctypes.c_int32),
+                ("initp", (ctypes.c_float * 4) * 8)]
 
 
 class Frontend(ctypes.Structure):

@@ -328,8 +328,14 @@ int64_t bsfit_batch_scratch_bytes(int32_t nseg) {
   return (((int64_t)nseg * 2 * 8) + 255) / 256 * 256;
 }
 
-int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scratch,
-                           int64_t scratch_bytes, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// The batched fit behind bsfit_batch_fit_device (starts null) and
+// bsfit_batch_fit_multistart_device (starts[i] for segment i).
+int batch_fit(const bsfit_segment* segs, const bsfit_starts* starts, int32_t nseg,
+              void* d_scratch, int64_t scratch_bytes, void* stream) {
   if (nseg < 0 || nseg > BSFIT_MAX_SEGMENTS) return BSFIT_E_INVALID;
   if (nseg == 0) return BSFIT_OK;
   if (!segs || !d_scratch || scratch_bytes < bsfit_batch_scratch_bytes(nseg)) return BSFIT_E_INVALID;
@@ -340,6 +346,11 @@ int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scra
     if (g.roi_size < 1 || g.roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
     if (g.nfits < 0) return BSFIT_E_INVALID;
     if (g.nfits > 0 && (!g.d_rois || !g.d_P || !g.d_CRLB || !g.d_LL)) return BSFIT_E_INVALID;
+    if (starts) {
+      const bsfit_starts& q = starts[i];
+      if (q.n_starts < 1 || q.n_starts > BSFIT_MAX_STARTS) return BSFIT_E_INVALID;
+      if (g.model->dev.fittype == 6) return BSFIT_E_UNSUPPORTED_FITTYPE;  // no initP
+    }
   }
   cudaStream_t st = (cudaStream_t)stream;
   unsigned long long* next = (unsigned long long*)d_scratch;
@@ -383,12 +394,35 @@ int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scra
       b.s = (int)g.roi_size;
       b.iterations = g.iterations;
       b.slot = order[j];  // counters stay in the caller's segment order
+      if (starts) {
+        const bsfit_starts& q = starts[order[j]];
+        b.n_starts = q.n_starts;
+        b.strict = q.strict ? 1 : 0;
+        for (int k = 0; k < q.n_starts; ++k)
+          for (int c = 0; c < 4; ++c) b.starts[k][c] = q.initp[k][c];
+      }
       if (b.s > a.s_max) a.s_max = b.s;
     }
-    e = bsfit::launch_batch(a, mode, st);
+    e = bsfit::launch_batch(a, mode, starts != nullptr, st);
     if (e != cudaSuccess) return cuda_status(e);
   }
   return BSFIT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scratch,
+                           int64_t scratch_bytes, void* stream) {
+  return batch_fit(segs, nullptr, nseg, d_scratch, scratch_bytes, stream);
+}
+
+int bsfit_batch_fit_multistart_device(const bsfit_segment* segs, const bsfit_starts* starts,
+                                      int32_t nseg, void* d_scratch, int64_t scratch_bytes,
+                                      void* stream) {
+  if (!starts) return BSFIT_E_INIT_P;
+  return batch_fit(segs, starts, nseg, d_scratch, scratch_bytes, stream);
 }
 
 int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t roi_size2,

@@ -1398,8 +1398,10 @@ __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) fit_kernel(FitArgs
 // segments' work counters (in segment order: the host sorts segments by
 // decreasing cost, so the largest ROIs start first and the tail is short),
 // fits them, and counts them done. The warp's shared memory is laid out for
-// the largest ROI of the batch.
-template <int MODE>
+// the largest ROI of the batch. MULTI: every ROI is fitted from its segment's
+// starts and the best log-likelihood kept (fit_and_store), in a separate
+// instantiation so the single-start kernel carries no start loop.
+template <int MODE, bool MULTI = false>
 __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) batch_kernel(const __grid_constant__ BatchArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
@@ -1437,7 +1439,15 @@ __global__ void __launch_bounds__(128, BSFIT_MINBLOCKS(MODE)) batch_kernel(const
     fa.strict = 0;
     fa.var = nullptr;
     fa.claim = nullptr;
-    fit_and_store<MODE, false>(fa, make_layout(MODE, g.s), ws, lane, (int64_t)i);
+    if constexpr (MULTI) {
+      fa.n_starts = g.n_starts;
+      fa.strict = g.strict;
+#pragma unroll 1
+      for (int k = 0; k < g.n_starts; ++k)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) fa.starts[k][j] = g.starts[k][j];
+    }
+    fit_and_store<MODE, MULTI>(fa, make_layout(MODE, g.s), ws, lane, (int64_t)i);
     if (lane == 0) atomicAdd(&a.done[g.slot], 1ull);
   }
 }
@@ -1512,13 +1522,13 @@ cudaError_t pick_launch(const void* kern, int per_warp, int* wpb, int* bps, int*
   return cudaSuccess;
 }
 
-cudaError_t launch_batch(const BatchArgs& a, int mode, cudaStream_t stream) {
+cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t stream) {
   if (a.nseg <= 0) return cudaSuccess;
   const int per_warp = warp_smem_floats(mode, a.s_max) * 4;
   void (*kern)(const BatchArgs) = nullptr;
-  if (mode == 6) kern = batch_kernel<6>;
-  else if (mode == 7) kern = batch_kernel<7>;
-  else if (mode == 8) kern = batch_kernel<8>;
+  if (mode == 6 && !multi) kern = batch_kernel<6>;
+  else if (mode == 7) kern = multi ? batch_kernel<7, true> : batch_kernel<7>;
+  else if (mode == 8) kern = multi ? batch_kernel<8, true> : batch_kernel<8>;
   else return cudaErrorInvalidValue;
   int wpb = 4, blocks_per_sm = 0, sms = 0;
   cudaError_t e = pick_launch((const void*)kern, per_warp, &wpb, &blocks_per_sm, &sms);

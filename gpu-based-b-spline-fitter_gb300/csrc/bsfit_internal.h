@@ -81,6 +81,11 @@ struct BatchSeg {
   int s;
   int iterations;
   int slot;  // index of this segment's counters in next[] / done[]
+  // multi-start (fit types 7, 8; the multi-start batched kernel only): the
+  // starts' initP vectors and the keep rule, as FitArgs
+  int n_starts;
+  int strict;
+  float starts[kMaxStarts][4];
 };
 
 struct BatchArgs {
@@ -121,7 +126,7 @@ cudaError_t widen_to_f64(const float* src, double* dst, int64_t total, int naxes
 int fit64_smem_bytes(int mode);
 
 int warp_smem_floats(int mode, int s, bool var = false);
-cudaError_t launch_batch(const BatchArgs& a, int mode, cudaStream_t stream);
+cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t stream);
 cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream);
 cudaError_t measure_fp32_peak(double* tflops);
 cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fisher,

@@ -188,6 +188,24 @@ int64_t bsfit_batch_scratch_bytes(int32_t nseg);
 int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scratch,
                            int64_t scratch_bytes, void* stream);
 
+/* Multi-start of the batched fit (fit types 7 and 8): starts[i] gives segment
+ * i's initP vectors (n_starts <= BSFIT_MAX_STARTS; z, w for fit type 7; z, w,
+ * u, g2 for 8) and keep rule; every ROI is fitted from each start inside the
+ * persistent launch and the best log-likelihood kept (a later start replaces
+ * the kept result when its LL is higher by at least 1e-4, or by more than
+ * 1e-4 with strict != 0), bit for bit the results of
+ * bsfit_fit_multistart_device on each segment. Fit type 6 segments return
+ * BSFIT_E_UNSUPPORTED_FITTYPE (no initP). */
+typedef struct bsfit_starts {
+  int32_t n_starts;
+  int32_t strict;
+  float initp[8][4];  /* BSFIT_MAX_STARTS x 4, unused entries ignored */
+} bsfit_starts;
+
+int bsfit_batch_fit_multistart_device(const bsfit_segment* segs, const bsfit_starts* starts,
+                                      int32_t nseg, void* d_scratch, int64_t scratch_bytes,
+                                      void* stream);
+
 /*
  * Serving form (no counterpart in the reference, whose GUI fits one block at a
  * time, MultiD_fitter/simplefitter_cspline.m:309-313): a continuous-batching

@@ -108,3 +108,52 @@ def test_multistart_rejects(bsfit_mod):
     with pytest.raises(bsfit_mod.BsfitError) as e:
         m4.fit_multistart_torch(r4, 30, np.zeros((2, 1), np.float32))
     assert e.value.status == 10
+
+
+@pytest.mark.parametrize("strict", [False, True])
+def test_batched_multistart_matches_plain(bsfit_mod, strict):
+    """Multi-start inside the persistent batched launch
+    (bsfit_batch_fit_multistart_device): 4D segments of two ROI sizes and a 5D
+    segment, each with its own starts, equal the plain fused multi-start of
+    each segment bit for bit."""
+    import torch
+    from bsfit import workloads as W
+    w13, w15 = W.workload_4d(600, sizes=(13, 15), stream=905)
+    w5 = W.workload_5d(96, stream=906)
+    z, w = float(w13.init_p[0]), float(w13.init_p[1])
+    st4a = np.array([[1.2 * z, w], [z, w], [0.8 * z, w]], np.float32)
+    st4b = np.array([[z, w], [0.9 * z, w]], np.float32)
+    s1 = w5.init_p.copy()
+    s1[1] = W.phi_to_w(np.pi / 3)
+    st5 = np.stack([w5.init_p, s1]).astype(np.float32)
+    m13 = bsfit_mod.Model(7, w13.coeff, init_p=w13.init_p)
+    m15 = bsfit_mod.Model(7, w15.coeff, init_p=w15.init_p)
+    m5 = bsfit_mod.Model(8, w5.coeff, coeff3=w5.coeff3, init_p=w5.init_p)
+    r13, r15, r5 = (torch.from_numpy(x.rois).cuda() for x in (w13, w15, w5))
+    entries = [(m13, r13, w13.iterations), (m15, r15, w15.iterations), (m5, r5, w5.iterations)]
+    starts = [st4a, st4b, st5]
+    b = bsfit_mod.Batch(entries, starts=starts, strict=strict)
+    outs = [_np(o) for o in b.run()]
+    plain = [_np(m.fit_multistart_torch(r, it, st, strict=strict))
+             for (m, r, it), st in zip(entries, starts)]
+    torch.cuda.synchronize()
+    for o, p in zip(outs, plain):
+        for a, c in zip(o, p):
+            assert np.array_equal(a, c, equal_nan=True)
+    claimed, done = b.counters()
+    assert list(done) == [len(w13.rois), len(w15.rois), len(w5.rois)]
+
+
+def test_batched_multistart_rejects(bsfit_mod):
+    import torch
+    from bsfit import BsfitError
+    from bsfit import workloads as W
+    w3 = W.workload_3d(64, s=13, stream=907)
+    m = bsfit_mod.Model(6, w3.coeff)
+    r = torch.from_numpy(w3.rois).cuda()
+    with pytest.raises(BsfitError):  # fit type 6 has no initP
+        bsfit_mod.Batch([(m, r, 30)], starts=[[[1.0, 2.0]]]).run()
+    w4 = W.workload_4d(64, sizes=(13,), stream=908)[0]
+    m4 = bsfit_mod.Model(7, w4.coeff, init_p=w4.init_p)
+    with pytest.raises(ValueError):
+        bsfit_mod.Batch([(m4, torch.from_numpy(w4.rois).cuda(), 60)], starts=[np.zeros((9, 2))])

@@ -458,15 +458,28 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
   // Pipeline: a copy stream uploads the coefficients and the ROIs chunk by
   // chunk; two compute streams fit the chunks alternately as their uploads
   // land, so chunk i + 1 uploads while chunk i fits and the tail of one fit
-  // launch overlaps the start of the next. Results come back in one copy at the
-  // end (the outputs are column-major over all ROIs). Device buffers come from
-  // the stream-ordered pool, so repeated calls allocate nothing.
+  // launch overlaps the start of the next. The first chunk is small, so the
+  // first fit starts after a short upload, and the chunks double from there
+  // (uploads run several times faster than fits, so they stay ahead). Each
+  // chunk's results go back to the host as soon as its fit ends, one strided
+  // copy per output (the outputs are column-major over all ROIs), so only the
+  // last chunk's copy remains after the last fit. Device buffers come from the
+  // stream-ordered pool, so repeated calls allocate nothing.
   CallStreams* cs = call_streams();
   if (!cs) return BSFIT_E_CUDA;
   cudaStream_t cp = cs->copy, c0 = cs->comp[0], c1 = cs->comp[1];
-  const int64_t chunk_min = 131072;
-  const int64_t nchunk = std::min<int64_t>(CallStreams::kEvents, std::max<int64_t>(1, nfits / chunk_min));
-  const int64_t chunk = (nfits + nchunk - 1) / nchunk;
+  int64_t cb[CallStreams::kEvents + 1];
+  int nchunk = 0;
+  {
+    const int64_t first_chunk = 16384;
+    int64_t b = 0, c = first_chunk;
+    while (b < nfits && nchunk < CallStreams::kEvents) {
+      cb[nchunk++] = b;
+      b += c;
+      c *= 2;
+    }
+    cb[nchunk] = nfits;
+  }
   float *d_rois = nullptr, *d_out = nullptr, *d_c = nullptr, *d_c3 = nullptr;
   cudaError_t e = cudaMallocAsync(&d_rois, in_bytes, cp);
   if (e == cudaSuccess) e = cudaMallocAsync(&d_out, out_bytes, cp);
@@ -486,9 +499,8 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
   a.CRLB = d_out + (size_t)nfits * (nv + 1);
   a.LL = a.CRLB + (size_t)nfits * nv;
   a.out_n = nfits;
-  for (int64_t i = 0; i < nchunk && e == cudaSuccess; ++i) {
-    const int64_t b = i * chunk, n = std::min(chunk, nfits - b);
-    if (n <= 0) break;
+  for (int i = 0; i < nchunk && e == cudaSuccess; ++i) {
+    const int64_t b = cb[i], n = cb[i + 1] - b;
     e = cudaMemcpyAsync(d_rois + (size_t)b * s2, imstack + (size_t)b * s2, (size_t)n * s2 * 4,
                         cudaMemcpyHostToDevice, cp);
     if (e == cudaSuccess) e = cudaEventRecord(cs->ev[i], cp);
@@ -501,15 +513,23 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
       e = bsfit::launch_fit(a, cs_i);
     }
   }
-  // join: c0 waits for c1's last launch, then copies the results back
+  // Results of each chunk, on the stream that fitted it (enqueued after every
+  // launch: a copy into pageable host memory returns only when it is done).
+  const size_t ld = (size_t)nfits * sizeof(float);
+  for (int i = 0; i < nchunk && e == cudaSuccess; ++i) {
+    const int64_t b = cb[i], n = cb[i + 1] - b;
+    cudaStream_t cs_i = (i & 1) ? c1 : c0;
+    e = cudaMemcpy2DAsync(P + b, ld, a.P + b, ld, (size_t)n * sizeof(float), nv + 1,
+                          cudaMemcpyDeviceToHost, cs_i);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(CRLB + b, ld, a.CRLB + b, ld, (size_t)n * sizeof(float), nv,
+                            cudaMemcpyDeviceToHost, cs_i);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(LL + b, a.LL + b, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, cs_i);
+  }
+  // join: c0 waits for c1's last copies
   if (e == cudaSuccess) e = cudaEventRecord(cs->join, c1);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(c0, cs->join, 0);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(P, a.P, (size_t)nfits * (nv + 1) * sizeof(float), cudaMemcpyDeviceToHost, c0);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(CRLB, a.CRLB, (size_t)nfits * nv * sizeof(float), cudaMemcpyDeviceToHost, c0);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(LL, a.LL, (size_t)nfits * sizeof(float), cudaMemcpyDeviceToHost, c0);
   // buffers were allocated on the copy stream: free them on c0 once the copy
   // stream's work is ordered before it (the chunk events already are)
   if (cudaEventRecord(cs->join, cp) == cudaSuccess) cudaStreamWaitEvent(c0, cs->join, 0);

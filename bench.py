@@ -60,38 +60,63 @@ def dist_env():
 
 
 class ClockSampler:
-    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region:
+    one nvidia-smi process streaming a line every 50 ms, started before the
+    region (so its start-up does not fall inside it), each line stamped on
+    arrival; the summary keeps the lines that arrived between entering and
+    leaving the region (the nearest one when the region is shorter than the
+    sampling period)."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 50
 
     def __init__(self, index=0):
         self.index = index
+        self.lines = []  # (arrival time, fields)
         self.samples = []
-        self._stop = threading.Event()
+        self._p = None
         self._t = None
+        self.t0 = self.t1 = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(
-                    ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                     "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if out.returncode == 0 and out.stdout.strip():
-                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self._p.stdout:
+            f = [x.strip() for x in line.strip().split(",")]
+            if len(f) >= 8:
+                self.lines.append((time.time(), f))
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self._p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+            deadline = time.time() + 5.0
+            while not self.lines and time.time() < deadline:
+                time.sleep(0.01)
+        except Exception:
+            self._p = None
+        self.t0 = time.time()
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        self.t1 = time.time()
+        if self._p is not None:
+            time.sleep(self.PERIOD_MS * 1.5e-3)
+            self._p.terminate()  # the process started above
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+            self._t.join(timeout=5)
+        inside = [f for t, f in self.lines if self.t0 <= t <= self.t1 + self.PERIOD_MS * 1e-3]
+        if not inside and self.lines:
+            mid = 0.5 * (self.t0 + self.t1)
+            inside = [min(self.lines, key=lambda x: abs(x[0] - mid))[1]]
+        self.samples = inside
 
     def summary(self):
         if not self.samples:
@@ -103,7 +128,7 @@ class ClockSampler:
                           if len(s) > 4 + i and s[4 + i].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.samples)}
+                "samples": len(self.samples), "period_ms": self.PERIOD_MS}
 
 
 def make_workload(n=N_ROIS, sizes=SIZES):

@@ -108,3 +108,37 @@ def test_4pi_rejects_short_inputs():
     with pytest.raises(bsfit.BsfitError) as e:
         _call4pi(s=52)
     assert e.value.status == 3
+
+
+def test_batch_entry_points_reject_before_any_device_work(lib):
+    """Argument checks of the batched entries that need no GPU: an empty batch
+    is a no-op, too many segments and a missing starts array are refused."""
+    from bsfit import _native
+    segs = (_native.Segment * 1)()
+    st = (_native.Starts * 1)()
+    assert lib.bsfit_batch_fit_device(None, 0, None, 0, None) == 0
+    assert lib.bsfit_batch_fit_device(segs, 49, None, 0, None) == 11
+    assert lib.bsfit_batch_fit_multistart_device(segs, None, 1, None, 0, None) == 10
+    assert lib.bsfit_batch_fit_multistart_device(segs, st, 0, None, 0, None) == 0
+    assert lib.bsfit_batch_fit_multistart_device(segs, st, 49, None, 0, None) == 11
+    assert lib.bsfit_batch_scratch_bytes(3) >= 3 * 16
+
+
+def test_fp64_entry_points_reject_before_any_device_work(lib):
+    """The FP64 entries refuse a missing model or arguments the reference's
+    mex refuses (ROI larger than 51, non-square, unsupported fit type) before
+    any CUDA call."""
+    d = np.zeros(3 * 52 * 52, np.float32)
+    out = np.zeros(100, np.float64)
+    p = out.ctypes.data
+    assert lib.bsfit_fit_f64_device(None, None, None, 13, 4, 10, p, p, p, None) == 11
+    dims = (np.ctypeslib.ctypes.c_int64 * 3)(29, 29, 64)
+    c = np.zeros(29 * 29 * 64, np.float32)
+    fp = np.ctypeslib.ctypes.POINTER(np.ctypeslib.ctypes.c_float)
+    args = lambda s1, s2, ft: (d.ctypes.data_as(fp), s1, s2, 3, ft, 10, c.ctypes.data_as(fp), 3,  # noqa: E731
+                               dims, None, 0, 1, None, 0, None, 0, None, p, p, p)
+    assert lib.bsfit_GPUmleFit_LM_multiD_f64(*args(52, 52, 6)) == 3   # SubregionSize
+    assert lib.bsfit_GPUmleFit_LM_multiD_f64(*args(13, 12, 6)) == 4   # SubregionShape
+    assert lib.bsfit_GPUmleFit_LM_multiD_f64(*args(13, 13, 3)) == 5   # unsupported fit type
+    assert lib.bsfit_GPUmleFit_LM_multiD_f64(None, 13, 13, 3, 6, 10, c.ctypes.data_as(fp), 3, dims,
+                                             None, 0, 1, None, 0, None, 0, None, p, p, p) == 2

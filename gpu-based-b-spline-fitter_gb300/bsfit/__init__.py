@@ -295,6 +295,23 @@ class Model4Pi:
             P.data_ptr(), C.data_ptr(), L.data_ptr(), st.cuda_stream), "bsfit_fit4pi_device")
         return P, C, L
 
+    def fit_f64_torch(self, rois, iterations, initZ, initPhi, dT, stream=None):
+        """The 4Pi fit in double (bsfit_fit4pi_f64_device): arguments as
+        fit_torch (dT required); float64 (P (7, N), CRLB (6, N), LL (N,))."""
+        import torch
+        assert rois.is_cuda and rois.dtype == torch.float32 and rois.is_contiguous()
+        n, s = rois.shape[1], rois.shape[-1]
+        z0, w0, dt = initZ.contiguous(), initPhi.contiguous(), dT.contiguous()
+        P = torch.empty((7, n), device=rois.device, dtype=torch.float64)
+        C = torch.empty((6, n), device=rois.device, dtype=torch.float64)
+        L = torch.empty((n,), device=rois.device, dtype=torch.float64)
+        st = stream if stream is not None else torch.cuda.current_stream(rois.device)
+        check(_native.lib().bsfit_fit4pi_f64_device(
+            self._h, rois.data_ptr(), s, n, int(iterations), dt.data_ptr(), z0.data_ptr(),
+            w0.data_ptr(), P.data_ptr(), C.data_ptr(), L.data_ptr(), st.cuda_stream),
+            "bsfit_fit4pi_f64_device")
+        return P, C, L
+
     def fit_multistart_torch(self, rois, iterations, initZ, initPhi, dT=None, strict=False,
                              stream=None):
         """Fused multi-start 4Pi fit: initZ, initPhi of shape (starts, N); the

@@ -812,26 +812,23 @@ int bsfit_fit_scmos_device(bsfit_model model, const float* d_rois, const float* 
 // of operations (the float build of the reference and the FP32 kernels take
 // some LM decisions differently from the double build; this one follows it).
 
-int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_var,
-                         int64_t roi_size, int64_t nfits, int32_t iterations, double* d_P,
-                         double* d_CRLB, double* d_LL, void* stream) {
-  if (!model) return BSFIT_E_INVALID;
-  const int ft = model->dev.fittype;
-  if (ft != 6 && ft != 7 && ft != 8) return BSFIT_E_UNSUPPORTED_FITTYPE;
-  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
-  if (nfits < 0) return BSFIT_E_INVALID;
-  if (nfits == 0) return BSFIT_OK;
-  if (!d_rois || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+}  // extern "C"
+
+namespace {
+
+// The double tables of a model (values and neighbour differences per axis),
+// made on first use and kept with the model.
+int ensure_f64_tables(bsfit_model model, cudaStream_t st) {
   const ModelDev& m = model->dev;
+  const int ft = m.fittype;
   int64_t total = 1;
   for (int i = 0; i < 5; ++i) total *= m.cd[i];
   const int64_t total3 = (int64_t)m.cd[0] * m.cd[1] * m.cd[2];
-  cudaStream_t st = (cudaStream_t)stream;
   {
     std::lock_guard<std::mutex> lock(model->f64_mu);
     if (!model->d_coeff64) {
       double *c = nullptr, *c3 = nullptr;
-      const int D = ft == 6 ? 3 : ft == 7 ? 4 : 5;
+      const int D = ft == 6 ? 3 : ft == 8 ? 5 : 4;  // 4: fit type 7 and 4Pi
       cudaError_t e = cudaMalloc(&c, (size_t)(D + 1) * total * sizeof(double));
       if (e == cudaSuccess) e = bsfit::widen_to_f64(model->d_coeff, c, total, D, m.st, st);
       if (e == cudaSuccess && ft == 8) {
@@ -849,6 +846,30 @@ int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_
       model->d_coeff64 = c;
     }
   }
+  return BSFIT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_var,
+                         int64_t roi_size, int64_t nfits, int32_t iterations, double* d_P,
+                         double* d_CRLB, double* d_LL, void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  const int ft = model->dev.fittype;
+  if (ft != 6 && ft != 7 && ft != 8) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  const ModelDev& m = model->dev;
+  int64_t total = 1;
+  for (int i = 0; i < 5; ++i) total *= m.cd[i];
+  const int64_t total3 = (int64_t)m.cd[0] * m.cd[1] * m.cd[2];
+  cudaStream_t st = (cudaStream_t)stream;
+  const int rc = ensure_f64_tables(model, st);
+  if (rc != BSFIT_OK) return rc;
   bsfit::Fit64Args a;
   std::memset(&a, 0, sizeof(a));
   a.m = m;
@@ -927,6 +948,42 @@ int bsfit_GPUmleFit_LM_multiD_f64(const float* imstack, int64_t roi_size, int64_
   if (rc != BSFIT_OK) return rc;
   if (e == cudaSuccess) e = e2;
   return cuda_status(e);
+}
+
+// 4Pi in double: the restated 4Pi fit (oracle/bsfit_oracle.cpp fit_4pi_roi)
+// in its order of operations, as bsfit_fit_f64_device does for fit types 6-8;
+// arguments as bsfit_fit4pi_device with double outputs.
+int bsfit_fit4pi_f64_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                            int64_t nfits, int32_t iterations, const float* d_dT,
+                            const float* d_initZ, const float* d_initPhi, double* d_P,
+                            double* d_CRLB, double* d_LL, void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  if (model->dev.fittype != bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_dT || !d_initZ || !d_initPhi || !d_P || !d_CRLB || !d_LL)
+    return BSFIT_E_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int rc = ensure_f64_tables(model, st);
+  if (rc != BSFIT_OK) return rc;
+  const ModelDev& m = model->dev;
+  bsfit::Fit64Args a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = m;
+  a.c = model->d_coeff64;
+  a.total = (int64_t)m.cd[0] * m.cd[1] * m.cd[2] * m.cd[3];
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  a.dT = d_dT;
+  a.z0 = d_initZ;
+  a.w0 = d_initPhi;
+  return cuda_status(bsfit::launch_fit64(a, st));
 }
 
 }  // extern "C"

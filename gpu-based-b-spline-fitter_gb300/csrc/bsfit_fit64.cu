@@ -45,15 +45,22 @@ template <int MODE>
 struct F64Traits;
 template <>
 struct F64Traits<6> {
-  static constexpr int D = 3, NV = 5, WPB = 4;
+  static constexpr int D = 3, NV = 5, WPB = 4, NCH = 1;
 };
 template <>
 struct F64Traits<7> {
-  static constexpr int D = 4, NV = 6, WPB = 1;
+  static constexpr int D = 4, NV = 6, WPB = 1, NCH = 1;
 };
 template <>
 struct F64Traits<8> {
-  static constexpr int D = 5, NV = 8, WPB = 1;
+  static constexpr int D = 5, NV = 8, WPB = 1, NCH = 1;
+};
+// 4Pi (the restatement in the oracle, oracle/bsfit_oracle.cpp fit_4pi_roi):
+// four channels of the 4D model at theta + dT[c], phase shifted by the
+// channel's shift and wrapped, summed into one likelihood.
+template <>
+struct F64Traits<kFit4Pi> {
+  static constexpr int D = 4, NV = 6, WPB = 1, NCH = k4PiChannels;
 };
 
 // Float literals of the reference (VC/CPUmleFit_LM/definitions.h:15, :23-24).
@@ -90,6 +97,14 @@ struct F64Layout {
   static constexpr int off_rows = off_ax + AX;
   static constexpr int per_warp = off_rows + ROWS + (ROWS & 1);
 };
+
+// Phase position wrapped into [1, 1 + P), P = nw - 1, by one period.
+__device__ __forceinline__ double wrap_phase64(double w, int nw) {
+  const double P = (double)(nw - 1);
+  if (w < 1.0) return w + P;
+  if (w >= (double)nw) return w - P;
+  return w;
+}
 
 __device__ __forceinline__ int floor_to_int64(double v) {
   const double f = floor(v);
@@ -247,8 +262,9 @@ __device__ __forceinline__ void pixel_model(const Coef& c, const int* n, const i
 struct Fit64Ctx {
   const Fit64Args* a;
   Coef c, c3;
-  const float* data;
+  const float* data;  // channel 0's pixels; channel c at data + c * nfits * s * s
   const float* var;
+  const float* dT;    // 4Pi: this ROI's [4][6] channel offsets
   int s, lane;
 };
 
@@ -360,9 +376,26 @@ struct Warp64 {
   // log-likelihood at st.nt with the current frame (:2714-2742).
   template <bool FISHER>
   __device__ void pass(const Fit64Ctx& cx, bool dup45) {
+    constexpr int NCH = F64Traits<MODE>::NCH;
     const int s = cx.s, s2 = s * s, lane = cx.lane;
     double acc[2] = {0.0, 0.0};
-    const double N = st.nt[2], bg = st.nt[3];
+    double N = st.nt[2], bg = st.nt[3];
+    const float* data = cx.data;
+#pragma unroll 1
+    for (int ch = 0; ch < NCH; ++ch) {
+    if constexpr (NCH > 1) {
+      // channel ch at theta + dT[ch], its phase shifted and wrapped
+      // (Model4Pi::prepare / pixel of the restatement)
+      double tc[NV];
+#pragma unroll
+      for (int t = 0; t < NV; ++t) tc[t] = st.nt[t] + (double)cx.dT[ch * NV + t];
+      const double tw = tc[5];
+      tc[5] = wrap_phase64(tw + (double)cx.a->m.shift[ch], cx.a->m.n[3]);
+      prepare(cx, tc);
+      N = tc[2];
+      bg = tc[3];
+      data = cx.data + (int64_t)ch * cx.a->nfits * s2;
+    }
     for (int r0 = 0; r0 < s2; r0 += 32) {
       const int q = r0 + lane;
       if (q < s2) {
@@ -370,11 +403,11 @@ struct Warp64 {
         double dudt[NV], model;
         pixel(cx, ii, jj, N, bg, dudt, &model);
         const int di = s * jj + ii;
-        double data = (double)cx.data[di];
+        double dval = (double)data[di];
         if (cx.var) {
           const double v = (double)cx.var[di];
           model += v;
-          data += v;
+          dval += v;
         }
         double* row = rows + lane * RW;
         int k = 1 + NV;
@@ -383,7 +416,7 @@ struct Warp64 {
           double term = 0.0, use = 0.0;
           if (model > 0) {
             use = 1.0;
-            term = (data > 0) ? ((data * log(model) - model) - data * log(data)) + data : -model;
+            term = (dval > 0) ? ((dval * log(model) - model) - dval * log(dval)) + dval : -model;
           }
           row[0] = term;
           row[1] = use;
@@ -395,14 +428,14 @@ struct Warp64 {
           // CPUmleFit_LM.cpp:2537-2560
           if (dup45) dudt[5] = dudt[4];
           double term;
-          if (data > 0) {
-            term = 2.0 * ((model - data) - data * log(model / data));
+          if (dval > 0) {
+            term = 2.0 * ((model - dval) - dval * log(model / dval));
           } else {
             term = 2.0 * model;
-            data = 0.0;
+            dval = 0.0;
           }
-          const double t1 = 1.0 - data / model;
-          const double t2 = data / (model * model);
+          const double t1 = 1.0 - dval / model;
+          const double t2 = dval / (model * model);
           row[0] = term;
 #pragma unroll
           for (int l = 0; l < NV; ++l) row[1 + l] = t1 * dudt[l];
@@ -431,6 +464,7 @@ struct Warp64 {
         acc[h] = a;
       }
       __syncwarp();
+    }
     }
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -526,10 +560,54 @@ __device__ void mat_inv64(double* M, double* Minv, double* diag) {
 
 // Initial guesses (CPUgaussLib.cpp:172-225, CPUmleFit_LM.cpp:2478-2482,
 // :2839-2850, :3237-3256), lane 0.
+// The single-channel rule on one plane: x, y, N, bg into t[0..3].
+__device__ void guess_plane(const float* d, int s, double* t) {
+  double tx = 0.0, ty = 0.0, ts = 0.0;
+  for (int ii = 0; ii < s; ii++)
+    for (int jj = 0; jj < s; jj++) {
+      const double v = (double)d[s * jj + ii];
+      tx = tx + v * (double)ii;
+      ty = ty + v * (double)jj;
+      ts = ts + v;
+    }
+  t[0] = tx / ts;
+  t[1] = ty / ts;
+  double maxn = 0.0, minbg = (double)10e10f;
+  for (int kk = 0; kk < s; kk++)
+    for (int ll = 0; ll < s; ll++) {
+      const double v = (double)d[kk * s + ll];
+      maxn = (maxn > v) ? maxn : v;
+      minbg = (minbg < v) ? minbg : v;
+    }
+  const double n0 = ((((maxn - minbg) * 2.0) * (double)kPIf) * 1.5) * 1.5;
+  t[2] = (0.0 > n0) ? 0.0 : n0;
+  t[3] = (minbg > 0.01) ? minbg : 0.01;
+}
+
 template <int MODE>
-__device__ void initial_theta(const Fit64Ctx& cx, LMState& st) {
+__device__ void initial_theta(const Fit64Ctx& cx, LMState& st, int64_t roi) {
   constexpr int NV = F64Traits<MODE>::NV;
   const int s = cx.s;
+  if constexpr (MODE == kFit4Pi) {
+    // mean over the channels of the single-channel rule, lateral offsets
+    // removed; z and phase per ROI (fit_4pi_roi of the restatement)
+    double sx = 0.0, sy = 0.0, sn = 0.0, sb = 0.0;
+    for (int c = 0; c < k4PiChannels; ++c) {
+      double t4[4];
+      guess_plane(cx.data + (int64_t)c * cx.a->nfits * s * s, s, t4);
+      sx = sx + (t4[0] - (double)cx.dT[c * NV + 0]);
+      sy = sy + (t4[1] - (double)cx.dT[c * NV + 1]);
+      sn = sn + t4[2];
+      sb = sb + t4[3];
+    }
+    st.nt[0] = sx / 4.0;
+    st.nt[1] = sy / 4.0;
+    st.nt[2] = sn / 4.0;
+    st.nt[3] = sb / 4.0;
+    st.nt[4] = (double)cx.a->z0[roi];
+    st.nt[5] = wrap_phase64((double)cx.a->w0[roi], cx.a->m.n[3]);
+    return;
+  }
   const float* d = cx.data;
   double tx = 0.0, ty = 0.0, ts = 0.0;
   for (int ii = 0; ii < s; ii++)
@@ -655,6 +733,7 @@ __device__ int lm_control(LMState& st, const ModelDev& m, int s) {
     st.nt[5] = dmax(st.nt[5], 0.0);
     st.nt[5] = dmin(st.nt[5], (double)m.n[3] - 0.5);
   }
+  if (MODE == kFit4Pi) st.nt[5] = wrap_phase64(st.nt[5], m.n[3]);
   if (MODE == 8) {
     if (st.nt[5] <= 1) st.nt[5] = (double)(m.n[3] - 2) + st.nt[5];
     else if (st.nt[5] > (double)(m.n[3] - 1)) st.nt[5] = (2.0 + st.nt[5]) - (double)m.n[3];
@@ -684,6 +763,9 @@ __device__ void init_state(LMState& st) {
     // :2434
     const double c[5] = {2.0, 2.0, 10000, 20, 20};
     for (int i = 0; i < NV; i++) st.nc[i] = st.oc[i] = c[i], st.fade[i] = 0.0;
+  } else if (MODE == kFit4Pi) {
+    const double c[6] = {1, 1, 10000, 20, 2, 2};
+    for (int i = 0; i < NV; i++) st.nc[i] = st.oc[i] = c[i], st.fade[i] = 0.5;
   } else if (MODE == 7) {
     // :2786-2788
     const double c[6] = {1.0, 1.0, 10000, 20, 2, 0.00001};
@@ -716,9 +798,10 @@ __global__ void __launch_bounds__(32 * F64Traits<MODE>::WPB, 1) fit64_kernel(
   for (int64_t roi = (int64_t)blockIdx.x * WPB + warp; roi < a.nfits; roi += nw) {
     cx.data = a.rois + roi * s2;
     cx.var = a.var ? a.var + roi * s2 : nullptr;
+    cx.dT = (MODE == kFit4Pi) ? a.dT + roi * (int64_t)(k4PiChannels * NV) : nullptr;
     if (lane == 0) {
       init_state<MODE>(st);
-      initial_theta<MODE>(cx, st);
+      initial_theta<MODE>(cx, st, roi);
       for (int i = 0; i < NV; i++) {
         st.ot[i] = st.nt[i];
         if (MODE == 8) st.oc[i] = st.nc[i];
@@ -727,7 +810,8 @@ __global__ void __launch_bounds__(32 * F64Traits<MODE>::WPB, 1) fit64_kernel(
     }
     __syncwarp();
     // Initial evaluation; fit type 7 copies dudt[4] into dudt[5] here only.
-    w.prepare(cx, st.nt);
+    // (4Pi prepares per channel inside the pass.)
+    if (MODE != kFit4Pi) w.prepare(cx, st.nt);
     w.template pass<false>(cx, MODE == 7);
     int kk = 0;
     for (; kk < a.iterations; kk++) {
@@ -737,14 +821,14 @@ __global__ void __launch_bounds__(32 * F64Traits<MODE>::WPB, 1) fit64_kernel(
       __syncwarp();
       if (act == kStop) break;
       if (act == kEval) {
-        w.prepare(cx, st.nt);
+        if (MODE != kFit4Pi) w.prepare(cx, st.nt);
         w.template pass<false>(cx, false);
       }
     }
     // CRLB and log-likelihood: types 6 and 7 re-prepare at the final theta;
     // type 8 keeps the frame, weights and g2 of its last evaluation
     // (CPUmleFit_LM.cpp:3568-3584).
-    if (MODE != 8) w.prepare(cx, st.nt);
+    if (MODE != 8 && MODE != kFit4Pi) w.prepare(cx, st.nt);
     w.template pass<true>(cx, false);
     if (lane == 0) {
       mat_inv64<NV>(st.M, st.Minv, st.diag);
@@ -808,6 +892,7 @@ int fit64_smem_bytes(int mode) {
     case 6: return F64Layout<6>::per_warp * F64Traits<6>::WPB * 8;
     case 7: return F64Layout<7>::per_warp * F64Traits<7>::WPB * 8;
     case 8: return F64Layout<8>::per_warp * F64Traits<8>::WPB * 8;
+    case kFit4Pi: return F64Layout<kFit4Pi>::per_warp * F64Traits<kFit4Pi>::WPB * 8;
     default: return 0;
   }
 }
@@ -830,6 +915,7 @@ cudaError_t launch_fit64(const Fit64Args& a, cudaStream_t stream) {
     case 6: return launch64<6>(a, stream);
     case 7: return launch64<7>(a, stream);
     case 8: return launch64<8>(a, stream);
+    case kFit4Pi: return launch64<kFit4Pi>(a, stream);
     default: return cudaErrorInvalidValue;
   }
 }

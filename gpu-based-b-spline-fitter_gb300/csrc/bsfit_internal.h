@@ -117,6 +117,11 @@ struct Fit64Args {
   double* P;
   double* CRLB;
   double* LL;
+  // 4Pi: rois [4][nfits][s][s], channel offsets dT [nfits][4][6], initial z
+  // and phase [nfits]
+  const float* dT;
+  const float* z0;
+  const float* w0;
 };
 
 cudaError_t launch_fit64(const Fit64Args& a, cudaStream_t stream);

@@ -404,6 +404,15 @@ int bsfit_GPUmleFit_LM_multiD_f64(const float* imstack, int64_t roi_size, int64_
                                   const int64_t* coeff3_dims, double* P, double* CRLB,
                                   double* LL);
 
+/* The 4Pi fit in double (the FP64 reference-precision kernel's 4Pi form):
+ * arguments as bsfit_fit4pi_device (d_dT required), double outputs P [7][nfits],
+ * CRLB [6][nfits], LL [nfits]; results bit-identical to this project's double
+ * restatement of the 4Pi fit (the reference ships only a compiled 4Pi mex). */
+int bsfit_fit4pi_f64_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                            int64_t nfits, int32_t iterations, const float* d_dT,
+                            const float* d_initZ, const float* d_initPhi, double* d_P,
+                            double* d_CRLB, double* d_LL, void* stream);
+
 /*
  * Frame -> ROI front end (the step before the fit in the reference's
  * acquisition loop, MultiD_fitter/simplefitter_cspline.m:197-319, with the peak

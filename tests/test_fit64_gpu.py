@@ -147,3 +147,29 @@ def test_f64_dropin_rejects(bsfit_mod):
         bsfit_mod.GPUmleFit_LM_multiD(w3.rois, 3, 10, w3.coeff, precision="f64")
     with pytest.raises(ValueError):
         bsfit_mod.GPUmleFit_LM_multiD(w3.rois, 6, 10, w3.coeff, precision="f16")
+
+
+def test_f64_4pi_bit_identical_to_restatement(bsfit_mod, oracle):
+    """The 4Pi fit in double (bsfit_fit4pi_f64_device) against the oracle's
+    FP64 4Pi restatement: the same parameters bit for bit on the 4Pi parity
+    workload (the reference's 4Pi fit exists only as a compiled mex, so the
+    restatement is the method; its likelihood is pinned to the reference's
+    fit type 7 in tests/test_4pi_oracle.py)."""
+    import torch
+    from bsfit import workloads as W
+    wl = W.workload_4pi(n=3000, stream=802)
+    ex = wl.extra
+    m = bsfit_mod.Model4Pi(wl.coeff, ex["phase_shift"])
+    cu = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()  # noqa: E731
+    P, C, L = m.fit_f64_torch(cu(wl.rois), wl.iterations, cu(ex["init_z"]), cu(ex["init_phi"]),
+                              cu(ex["dT"]))
+    torch.cuda.synchronize()
+    P, C, L = P.cpu().numpy().T, C.cpu().numpy().T, L.cpu().numpy()
+    R, RC, RL = oracle.fit4pi(wl.rois, wl.iterations, wl.coeff, ex["dT"], ex["init_z"],
+                              ex["init_phi"], ex["phase_shift"], precision="f64",
+                              threads=os.cpu_count() or 1)
+    same = np.all(P == R, axis=1)
+    ok = tol_pass(P, C, R, RC, 6)
+    print(f"4Pi: {same.mean():.4f} bit-identical, {ok.mean():.4f} within tolerance")
+    assert same.mean() >= 0.99, same.mean()
+    assert np.median(np.abs(L - RL)) <= 1e-9 * np.median(np.abs(RL))

@@ -359,6 +359,27 @@ class Model4Pi:
             pass
 
 
+def _starts_array(starts, n_entries, strict):
+    """bsfit_starts per entry from sequences of initP vectors (None or an
+    empty sequence: one start from the model's initP)."""
+    if len(starts) != n_entries:
+        raise ValueError("one starts sequence per entry")
+    st = (_native.Starts * n_entries)()
+    for k, sv in enumerate(starts):
+        st[k].strict = int(bool(strict))
+        if sv is None or len(sv) == 0:
+            st[k].n_starts = 0
+            continue
+        a = np.atleast_2d(np.asarray(sv, np.float32))
+        if not 1 <= a.shape[0] <= 8 or a.shape[1] > 4:
+            raise ValueError("1 to 8 starts of at most 4 values per entry")
+        st[k].n_starts = a.shape[0]
+        for i in range(a.shape[0]):
+            for j in range(a.shape[1]):
+                st[k].initp[i][j] = float(a[i, j])
+    return st
+
+
 class Batch:
     """Batched fit of ROI segments (mixed ROI sizes and models) with one
     persistent launch per fit type. Each entry: (model, rois_cuda_tensor,
@@ -391,19 +412,7 @@ class Batch:
         self._segs = segs
         self._starts = None
         if starts is not None:
-            if len(starts) != len(self.entries):
-                raise ValueError("one starts sequence per entry")
-            st = (_native.Starts * len(self.entries))()
-            for k, sv in enumerate(starts):
-                a = np.atleast_2d(np.asarray(sv, np.float32))
-                if not 1 <= a.shape[0] <= 8 or a.shape[1] > 4:
-                    raise ValueError("1 to 8 starts of at most 4 values per entry")
-                st[k].n_starts = a.shape[0]
-                st[k].strict = int(bool(strict))
-                for i in range(a.shape[0]):
-                    for j in range(a.shape[1]):
-                        st[k].initp[i][j] = float(a[i, j])
-            self._starts = st
+            self._starts = _starts_array(starts, len(self.entries), strict)
         nb = _native.lib().bsfit_batch_scratch_bytes(len(self.entries))
         self.scratch = torch.zeros((max(nb, 256) // 8,), dtype=torch.int64, device=dev)
 
@@ -446,7 +455,10 @@ class Server:
         self._live = {}
         self._done = {}  # results collected by poll() and not yet taken by wait()
 
-    def submit(self, entries):
+    def submit(self, entries, starts=None, strict=False):
+        """Submit one request: entries (model, host ROIs, iterations); starts:
+        optional per-entry initP sequences (None or [] for one start), fitted
+        with the multi-start rule inside the batched launch."""
         import torch
         segs = (_native.HostSegment * len(entries))()
         keep = []
@@ -466,16 +478,25 @@ class Server:
             segs[k].nfits = n
             segs[k].iterations = int(it)
             segs[k].P, segs[k].CRLB, segs[k].LL = P.data_ptr(), C.data_ptr(), L.data_ptr()
-        rid = np.ctypeslib.ctypes.c_int64()
-        check(_native.lib().bsfit_server_submit(self._h, np.ctypeslib.ctypes.cast(segs, np.ctypeslib.ctypes.c_void_p),
-                                                len(entries), np.ctypeslib.ctypes.byref(rid)),
-              "bsfit_server_submit")
+        ct = np.ctypeslib.ctypes
+        rid = ct.c_int64()
+        if starts is None:
+            check(_native.lib().bsfit_server_submit(self._h, ct.cast(segs, ct.c_void_p),
+                                                    len(entries), ct.byref(rid)),
+                  "bsfit_server_submit")
+        else:
+            st = _starts_array(starts, len(entries), strict)
+            keep.append(st)
+            check(_native.lib().bsfit_server_submit_multistart(
+                self._h, ct.cast(segs, ct.c_void_p), ct.cast(st, ct.c_void_p), len(entries),
+                ct.byref(rid)), "bsfit_server_submit_multistart")
         self._live[rid.value] = (segs, keep)
         return rid.value
 
     def _results(self, rid):
         segs, keep = self._live.pop(rid)
-        return [(P.numpy().T.copy(), C.numpy().T.copy(), L.numpy().copy()) for m, r, P, C, L in keep]
+        return [(P.numpy().T.copy(), C.numpy().T.copy(), L.numpy().copy())
+                for m, r, P, C, L in (k for k in keep if isinstance(k, tuple))]
 
     def poll(self):
         ct = np.ctypeslib.ctypes

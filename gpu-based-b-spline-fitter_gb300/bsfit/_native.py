@@ -50,6 +50,9 @@ SIGNATURES = {
     "bsfit_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "bsfit_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                            ctypes.POINTER(ctypes.c_int64)]),
+    "bsfit_server_submit_multistart": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+        ctypes.POINTER(ctypes.c_int64)]),
     "bsfit_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                          ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
     "bsfit_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double]),

@@ -348,8 +348,9 @@ int batch_fit(const bsfit_segment* segs, const bsfit_starts* starts, int32_t nse
     if (g.nfits > 0 && (!g.d_rois || !g.d_P || !g.d_CRLB || !g.d_LL)) return BSFIT_E_INVALID;
     if (starts) {
       const bsfit_starts& q = starts[i];
-      if (q.n_starts < 1 || q.n_starts > BSFIT_MAX_STARTS) return BSFIT_E_INVALID;
-      if (g.model->dev.fittype == 6) return BSFIT_E_UNSUPPORTED_FITTYPE;  // no initP
+      if (q.n_starts < 0 || q.n_starts > BSFIT_MAX_STARTS) return BSFIT_E_INVALID;
+      // fit type 6 has no initP: one start, fitted by the single-start kernel
+      if (g.model->dev.fittype == 6 && q.n_starts > 1) return BSFIT_E_UNSUPPORTED_FITTYPE;
     }
   }
   cudaStream_t st = (cudaStream_t)stream;
@@ -403,7 +404,7 @@ int batch_fit(const bsfit_segment* segs, const bsfit_starts* starts, int32_t nse
       }
       if (b.s > a.s_max) a.s_max = b.s;
     }
-    e = bsfit::launch_batch(a, mode, starts != nullptr, st);
+    e = bsfit::launch_batch(a, mode, starts != nullptr && mode != 6, st);
     if (e != cudaSuccess) return cuda_status(e);
   }
   return BSFIT_OK;

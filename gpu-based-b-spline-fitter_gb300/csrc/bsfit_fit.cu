@@ -1359,7 +1359,8 @@ __device__ __forceinline__ void fit_and_store(const FitArgs& a, const WarpLayout
     // one call site for all starts (a second inlined copy of the fit would
     // double the kernel's instruction footprint)
     RoiResult best{0.0f, 0.0f, 0.0f, 0};
-    for (int k = 0; k < a.n_starts; ++k) {
+    const int ns = a.n_starts > 0 ? a.n_starts : 1;  // 0: the model's initP alone
+    for (int k = 0; k < ns; ++k) {
       const RoiResult r = fit_roi<MODE>(a, L, ws, lane, roi, k);
       const float d = r.ll - best.ll;
       if (k == 0 || (a.strict ? (d > 1e-4f) : (d >= 1e-4f))) best = r;

@@ -90,6 +90,7 @@ class Arena {
 struct Request {
   int64_t id = 0;
   std::vector<bsfit_host_segment> segs;
+  std::vector<bsfit_starts> starts;  // empty: single start
   int64_t bytes = 0;       // arena bytes
   int64_t offset = -1;     // arena offset
   int slot = -1;
@@ -167,8 +168,11 @@ int launch_request(bsfit_server_s* s, Request* r) {
     d.d_LL = d.d_CRLB + g.nfits * nv;
   }
   if (e != cudaSuccess) return cuda_status_s(e);
-  int stt = bsfit_batch_fit_device(dsegs.data(), (int32_t)dsegs.size(), scratch,
-                                   bsfit_batch_scratch_bytes((int32_t)dsegs.size()), st);
+  const int64_t sb = bsfit_batch_scratch_bytes((int32_t)dsegs.size());
+  int stt = r->starts.empty()
+                ? bsfit_batch_fit_device(dsegs.data(), (int32_t)dsegs.size(), scratch, sb, st)
+                : bsfit_batch_fit_multistart_device(dsegs.data(), r->starts.data(),
+                                                    (int32_t)dsegs.size(), scratch, sb, st);
   if (stt != BSFIT_OK) return stt;
   for (size_t i = 0; i < r->segs.size(); ++i) {
     const bsfit_host_segment& g = r->segs[i];
@@ -272,17 +276,29 @@ int bsfit_server_destroy(bsfit_server s) {
 
 int bsfit_server_submit(bsfit_server s, const bsfit_host_segment* segs, int32_t nseg,
                         int64_t* request_id) {
+  return bsfit_server_submit_multistart(s, segs, nullptr, nseg, request_id);
+}
+
+int bsfit_server_submit_multistart(bsfit_server s, const bsfit_host_segment* segs,
+                                   const bsfit_starts* starts, int32_t nseg,
+                                   int64_t* request_id) {
   if (!s || !segs || nseg < 1 || nseg > BSFIT_MAX_SEGMENTS || !request_id) return BSFIT_E_INVALID;
   for (int i = 0; i < nseg; ++i) {
     const bsfit_host_segment& g = segs[i];
     if (!g.model || g.nfits < 0 || (g.nfits > 0 && (!g.rois || !g.P || !g.CRLB || !g.LL)))
       return BSFIT_E_INVALID;
     if (g.roi_size < 1 || g.roi_size > 51) return BSFIT_E_SUBREGION_SIZE;
+    if (starts) {
+      if (starts[i].n_starts < 0 || starts[i].n_starts > BSFIT_MAX_STARTS) return BSFIT_E_INVALID;
+      if (bsfit_model_fittype(g.model) == 6 && starts[i].n_starts > 1)
+        return BSFIT_E_UNSUPPORTED_FITTYPE;
+    }
   }
   std::lock_guard<std::mutex> lock(s->mu);
   Request* r = new (std::nothrow) Request;
   if (!r) return BSFIT_E_NOT_ENOUGH_MEMORY;
   r->segs.assign(segs, segs + nseg);
+  if (starts) r->starts.assign(starts, starts + nseg);
   r->bytes = request_bytes(r->segs);
   if (r->bytes > s->arena.size()) {
     delete r;

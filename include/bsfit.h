@@ -194,8 +194,10 @@ int bsfit_batch_fit_device(const bsfit_segment* segs, int32_t nseg, void* d_scra
  * persistent launch and the best log-likelihood kept (a later start replaces
  * the kept result when its LL is higher by at least 1e-4, or by more than
  * 1e-4 with strict != 0), bit for bit the results of
- * bsfit_fit_multistart_device on each segment. Fit type 6 segments return
- * BSFIT_E_UNSUPPORTED_FITTYPE (no initP). */
+ * bsfit_fit_multistart_device on each segment. n_starts = 0 fits the segment
+ * once from its model's initP (the results of bsfit_batch_fit_device). Fit
+ * type 6 has no initP: its segments take n_starts <= 1 and are fitted once;
+ * more starts return BSFIT_E_UNSUPPORTED_FITTYPE. */
 typedef struct bsfit_starts {
   int32_t n_starts;
   int32_t strict;
@@ -234,6 +236,12 @@ typedef struct bsfit_server_s* bsfit_server;
 
 int bsfit_server_create(int32_t max_inflight, int64_t arena_bytes, bsfit_server* out);
 int bsfit_server_destroy(bsfit_server server);
+/* As bsfit_server_submit, with per-segment starts (bsfit_starts, see
+ * bsfit_batch_fit_multistart_device): the request's fits run the callers'
+ * multi-start inside the batched launch. */
+int bsfit_server_submit_multistart(bsfit_server server, const bsfit_host_segment* segs,
+                                   const bsfit_starts* starts, int32_t nseg,
+                                   int64_t* request_id);
 /* Non-blocking: admits the request or queues it; BSFIT_E_NOT_ENOUGH_MEMORY if it
  * can never fit the arena. */
 int bsfit_server_submit(bsfit_server server, const bsfit_host_segment* segs, int32_t nseg,

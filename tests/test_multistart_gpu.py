@@ -151,8 +151,13 @@ def test_batched_multistart_rejects(bsfit_mod):
     w3 = W.workload_3d(64, s=13, stream=907)
     m = bsfit_mod.Model(6, w3.coeff)
     r = torch.from_numpy(w3.rois).cuda()
-    with pytest.raises(BsfitError):  # fit type 6 has no initP
-        bsfit_mod.Batch([(m, r, 30)], starts=[[[1.0, 2.0]]]).run()
+    with pytest.raises(BsfitError):  # fit type 6 has no initP: at most one start
+        bsfit_mod.Batch([(m, r, 30)], starts=[[[1.0, 2.0], [3.0, 4.0]]]).run()
+    # one start (or none) on a 3D segment is its plain fit
+    one = [x.cpu().numpy() for x in bsfit_mod.Batch([(m, r, 30)], starts=[[]]).run()[0]]
+    plain = [x.cpu().numpy() for x in m.fit_torch(r, 30)]
+    for a_, b_ in zip(one, plain):
+        assert np.array_equal(a_, b_, equal_nan=True)
     w4 = W.workload_4d(64, sizes=(13,), stream=908)[0]
     m4 = bsfit_mod.Model(7, w4.coeff, init_p=w4.init_p)
     with pytest.raises(ValueError):

@@ -93,3 +93,40 @@ def test_serving_budget_and_timeout(bsfit_mod):
     assert st in (0, 12)  # done already, or BSFIT_E_TIMEOUT
     srv.wait(rid, timeout=120.0)
     srv.close()
+
+
+def test_serving_multistart_matches_plain(bsfit_mod):
+    """A request with per-segment starts (bsfit_server_submit_multistart):
+    its 4D and 5D segments equal the plain fused multi-start bit for bit, a
+    4D segment with no starts and a 3D segment equal the single-start fits."""
+    import torch
+    from bsfit import workloads as W
+    w3 = W.workload_3d(800, s=13, stream=820)
+    w4 = W.workload_4d(400, sizes=(13,), stream=821)[0]
+    w5 = W.workload_5d(48, stream=822)
+    z, w = float(w4.init_p[0]), float(w4.init_p[1])
+    st4 = np.array([[1.2 * z, w], [z, w], [0.8 * z, w]], np.float32)
+    s1 = w5.init_p.copy()
+    s1[1] = W.phi_to_w(np.pi / 3)
+    st5 = np.stack([w5.init_p, s1]).astype(np.float32)
+    m3 = bsfit_mod.Model(6, w3.coeff)
+    m4 = bsfit_mod.Model(7, w4.coeff, init_p=w4.init_p)
+    m5 = bsfit_mod.Model(8, w5.coeff, coeff3=w5.coeff3, init_p=w5.init_p)
+    srv = bsfit_mod.Server(max_inflight=2, arena_bytes=64 << 20)
+    entries = [(m3, w3.rois, w3.iterations), (m4, w4.rois, w4.iterations),
+               (m5, w5.rois, w5.iterations), (m4, w4.rois, w4.iterations)]
+    rid = srv.submit(entries, starts=[None, st4, st5, []], strict=False)
+    res = srv.wait(rid, timeout=120.0)
+    np_ = lambda t: tuple(x.cpu().numpy() for x in t)  # noqa: E731
+    ref = [
+        np_(m3.fit_torch(torch.from_numpy(w3.rois).cuda(), w3.iterations)),
+        np_(m4.fit_multistart_torch(torch.from_numpy(w4.rois).cuda(), w4.iterations, st4)),
+        np_(m5.fit_multistart_torch(torch.from_numpy(w5.rois).cuda(), w5.iterations, st5)),
+        np_(m4.fit_torch(torch.from_numpy(w4.rois).cuda(), w4.iterations)),
+    ]
+    torch.cuda.synchronize()
+    for (Ps, Cs, Ls), (P, C, L) in zip(res, ref):
+        assert np.array_equal(Ps, P.T, equal_nan=True)
+        assert np.array_equal(Cs, C.T, equal_nan=True)
+        assert np.array_equal(Ls, L, equal_nan=True)
+    srv.close()

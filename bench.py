@@ -627,11 +627,18 @@ def bench_gpu(args):
     # measured its bytes against the algorithmic 4 s^2 + 48 B per ROI; the
     # step's traffic is that ratio times the step's algorithmic bytes.
     traffic = None
+    issue = None
     tpath = os.path.join(ROOT, "profiles", "traffic_batch_kernel_3d.json")
     if os.path.exists(tpath):
         try:
-            ratio = float(json.load(open(tpath))["measured_over_algorithmic"])
+            prof = json.load(open(tpath))
+            ratio = float(prof["measured_over_algorithmic"])
             traffic = ratio * sum((4 * g.roi_size ** 2 + 48) * len(g.rois) for g in groups)
+            # The binding limit of this kernel is instruction issue, not FMA
+            # throughput: the fraction of the SM's issue rate it sustains.
+            issue = {"ipc": prof["ipc"], "max_ipc": prof["max_ipc"],
+                     "frac": prof["ipc"] / prof["max_ipc"],
+                     "source": "ncu, profiles/batch_kernel_3d_200k.md"}
         except Exception:
             traffic = None
     line = {
@@ -649,7 +656,8 @@ def bench_gpu(args):
                      "peak_source": "measured FP32 FMA throughput on this device "
                                     "(bsfit_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                      "flops_per_step": flops, "kernel_ms_per_step": kernel_ms,
-                     "per": "launch (the batched step is one persistent launch over all sizes)"},
+                     "per": "launch (the batched step is one persistent launch over all sizes)",
+                     "issue": issue},
         "plain_form": {"value": n_step / (plain_ms * 1e-3), "unit": "fits/s",
                        "launches_per_step": len(groups),
                        "kernel_ms_by_size": dict(zip([str(s) for s in SIZES], per_launch))},

@@ -2,8 +2,8 @@
 // types 6, 7 and 8 of CPUmleFit_LM / GPUmleFit_LM_multiD).
 //
 // THIS IS TEST INFRASTRUCTURE. It is the checker for the CUDA fitter: only the
-// tests, the smoke check and the CPU-baseline leg of the benchmark load it. No
-// product path links, calls or falls back to it.
+// tests, the smoke check, the CPU-baseline leg of the benchmark and its
+// reference arm load it. No product path links, calls or falls back to it.
 //
 // Every function restates the reference CPU method step by step, including the
 // places where the reference's C++ promotes an expression to double (the

@@ -79,6 +79,18 @@ def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, s
     return P.T, C.T, L
 
 
+def CPUmleFit_LM(imstack, fittype, iterations=50, coeff=None, varmap=0, silent=1, initP=None,
+                 coeff3=None, out=None, precision="f32"):
+    """The reference's CPU mex has the same call as GPUmleFit_LM_multiD
+    (VC/CPUmleFit_LM/mexFunction.cpp:130-263), and the CUDA kernels here follow
+    the CPU method (its initial guesses, clamps, bounds and consistent x/y use),
+    so a CPUmleFit_LM caller switches by name: this is GPUmleFit_LM_multiD.
+    precision="f64" returns the CPU method's double-precision results bit for
+    bit."""
+    return GPUmleFit_LM_multiD(imstack, fittype, iterations, coeff, varmap, silent, initP, coeff3,
+                               out=out, precision=precision)
+
+
 class Model:
     """A PSF model whose coefficient tables stay resident on the device."""
 

@@ -142,3 +142,11 @@ def test_fp64_entry_points_reject_before_any_device_work(lib):
     assert lib.bsfit_GPUmleFit_LM_multiD_f64(*args(13, 13, 3)) == 5   # unsupported fit type
     assert lib.bsfit_GPUmleFit_LM_multiD_f64(None, 13, 13, 3, 6, 10, c.ctypes.data_as(fp), 3, dims,
                                              None, 0, 1, None, 0, None, 0, None, p, p, p) == 2
+
+
+def test_cpu_call_name_is_the_drop_in():
+    import inspect
+    import bsfit
+    a = inspect.signature(bsfit.CPUmleFit_LM).parameters
+    b = inspect.signature(bsfit.GPUmleFit_LM_multiD).parameters
+    assert list(a) == list(b)

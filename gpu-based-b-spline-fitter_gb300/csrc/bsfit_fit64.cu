@@ -370,32 +370,15 @@ struct Warp64 {
     }
   }
 
-  // One pass over the ROI. FISHER = false: deviance, gradient and Hessian at
-  // st.nt (CPUmleFit_LM.cpp:2530-2560), prepared first; dup45 copies dudt[4]
-  // into dudt[5] (fit type 7's initial pass). FISHER = true: Fisher matrix and
-  // log-likelihood at st.nt with the current frame (:2714-2742).
+  // The pixels of one plane, in the reference's order (ii outer, jj inner), 32
+  // at a time: each lane publishes its pixel's terms in a row (the deviance
+  // term, t1 * dudt[l] and (t2 * dudt[l]) * dudt[m]; or the log-likelihood term,
+  // its use flag and (dudt[m] * dudt[l]) / model), then every owner adds its
+  // entry of the rows in pixel order to acc.
   template <bool FISHER>
-  __device__ void pass(const Fit64Ctx& cx, bool dup45) {
-    constexpr int NCH = F64Traits<MODE>::NCH;
+  __device__ void accumulate_plane(const Fit64Ctx& cx, const float* data, double N, double bg,
+                                   bool dup45, double (&acc)[2]) {
     const int s = cx.s, s2 = s * s, lane = cx.lane;
-    double acc[2] = {0.0, 0.0};
-    double N = st.nt[2], bg = st.nt[3];
-    const float* data = cx.data;
-#pragma unroll 1
-    for (int ch = 0; ch < NCH; ++ch) {
-    if constexpr (NCH > 1) {
-      // channel ch at theta + dT[ch], its phase shifted and wrapped
-      // (Model4Pi::prepare / pixel of the restatement)
-      double tc[NV];
-#pragma unroll
-      for (int t = 0; t < NV; ++t) tc[t] = st.nt[t] + (double)cx.dT[ch * NV + t];
-      const double tw = tc[5];
-      tc[5] = wrap_phase64(tw + (double)cx.a->m.shift[ch], cx.a->m.n[3]);
-      prepare(cx, tc);
-      N = tc[2];
-      bg = tc[3];
-      data = cx.data + (int64_t)ch * cx.a->nfits * s2;
-    }
     for (int r0 = 0; r0 < s2; r0 += 32) {
       const int q = r0 + lane;
       if (q < s2) {
@@ -465,6 +448,32 @@ struct Warp64 {
       }
       __syncwarp();
     }
+  }
+
+  // One pass over the ROI. FISHER = false: deviance, gradient and Hessian at
+  // st.nt (CPUmleFit_LM.cpp:2530-2560) with the frame the caller prepared;
+  // dup45 copies dudt[4] into dudt[5] (fit type 7's initial pass). FISHER =
+  // true: Fisher matrix and log-likelihood at st.nt with the current frame
+  // (:2714-2742). 4Pi: every channel at theta + dT[c], its phase shifted by the
+  // channel's shift and wrapped, prepared here (Model4Pi of the restatement),
+  // channel outer and pixel inner into the same sums.
+  template <bool FISHER>
+  __device__ void pass(const Fit64Ctx& cx, bool dup45) {
+    constexpr int NCH = F64Traits<MODE>::NCH;
+    double acc[2] = {0.0, 0.0};
+    if constexpr (NCH == 1) {
+      accumulate_plane<FISHER>(cx, cx.data, st.nt[2], st.nt[3], dup45, acc);
+    } else {
+      const int64_t plane = (int64_t)cx.a->nfits * cx.s * cx.s;
+#pragma unroll 1
+      for (int ch = 0; ch < NCH; ++ch) {
+        double tc[NV];
+#pragma unroll
+        for (int t = 0; t < NV; ++t) tc[t] = st.nt[t] + (double)cx.dT[ch * NV + t];
+        tc[5] = wrap_phase64(tc[5] + (double)cx.a->m.shift[ch], cx.a->m.n[3]);
+        prepare(cx, tc);
+        accumulate_plane<FISHER>(cx, cx.data + ch * plane, tc[2], tc[3], dup45, acc);
+      }
     }
 #pragma unroll
     for (int h = 0; h < 2; ++h) {

@@ -143,7 +143,8 @@ def bench_kernel_only(args):
     3D (default): one plain launch per size group, or with --batched one
     persistent batched launch per step; --model 5d: fit type 8 on --rois ROIs
     of 17 px; --model 4pi: the 4Pi fit of --rois ROIs of four 13 px channels;
-    --model 3d64: the FP64 reference-precision kernel on --rois 3D ROIs of 13 px."""
+    --model 3d64: the FP64 reference-precision kernel on --rois 3D ROIs of 13 px;
+    --model 4d: fit type 7 on --rois ROIs of 13 px."""
     import torch
     import bsfit
     from bsfit import workloads as W
@@ -159,6 +160,17 @@ def bench_kernel_only(args):
                 m5.fit_torch(r5, w5.iterations, stream=stream)
         stream.synchronize()
         print(json.dumps({"profile_case": True, "model": "5d", "rois": len(w5.rois),
+                          "launches": launches}))
+        return 0
+    if args.model == "4d":
+        w4 = W.workload_4d(args.rois, sizes=(13,), stream=6)[0]
+        m4 = bsfit.Model(7, w4.coeff, init_p=w4.init_p)
+        r4 = torch.from_numpy(w4.rois).to(dev)
+        with torch.cuda.stream(stream):
+            for _ in range(launches):
+                m4.fit_torch(r4, w4.iterations, stream=stream)
+        stream.synchronize()
+        print(json.dumps({"profile_case": True, "model": "4d", "rois": len(w4.rois),
                           "launches": launches}))
         return 0
     if args.model == "3d64":
@@ -690,7 +702,7 @@ def main():
                     help="profiling case: only the fit launches of --rois ROIs of --sizes")
     ap.add_argument("--rois", type=int, default=N_ROIS)
     ap.add_argument("--batched", action="store_true", help="kernel-only: the batched form")
-    ap.add_argument("--model", default="3d", choices=["3d", "5d", "4pi", "3d64"],
+    ap.add_argument("--model", default="3d", choices=["3d", "4d", "5d", "4pi", "3d64"],
                     help="kernel-only: model")
     ap.add_argument("--sizes", type=int, nargs="+", default=list(SIZES))
     ap.add_argument("--rois-5d", type=int, default=50000, help="ROIs of the 5D 17 px figure")

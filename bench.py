@@ -568,6 +568,23 @@ def bench_gpu(args):
             b5.record(stream)
         stream.synchronize()
         fits_5d17 = len(w5.rois) / (a5.elapsed_time(b5) / 2 * 1e-3)
+    # 4D colour (fit type 7, 13 px, 60 iterations): the serving stream's
+    # largest share.
+    fits_4d13 = None
+    if not args.no_4d:
+        from bsfit import workloads as W
+        w7 = W.workload_4d(args.rois_4d, sizes=(13,), stream=6)[0]
+        m7 = bsfit.Model(7, w7.coeff, init_p=w7.init_p)
+        r7 = torch.from_numpy(w7.rois).to(dev)
+        with torch.cuda.stream(stream):
+            m7.fit_torch(r7, w7.iterations, stream=stream)
+            a7, b7 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a7.record(stream)
+            for _ in range(2):
+                m7.fit_torch(r7, w7.iterations, stream=stream)
+            b7.record(stream)
+        stream.synchronize()
+        fits_4d13 = len(w7.rois) / (a7.elapsed_time(b7) / 2 * 1e-3)
     # 4Pi (four channels of 13 px, 100 iterations, one phase start), the
     # reference demo's fit on its own synthetic workload.
     fits_4pi = None
@@ -677,7 +694,9 @@ def bench_gpu(args):
                          "kind": "port",
                          "sample": f"{cpu_n} ROIs (1.6% of each size group), FP32 oracle port of "
                                    f"the reference CPU fitter, OpenMP over ROIs"},
-        "fits_per_s": {"3d_13px": fits_3d13, "5d_17px": fits_5d17,
+        "fits_per_s": {"3d_13px": fits_3d13, "4d_13px": fits_4d13,
+                       "4d_workload": f"{args.rois_4d} ROIs 13x13, fit type 7, 60 iterations",
+                       "5d_17px": fits_5d17,
                        "5d_workload": f"{args.rois_5d} ROIs 17x17, fit type 8, 60 iterations",
                        "4pi_13px": fits_4pi,
                        "4pi_workload": f"{args.rois_4pi} ROIs of 4 channels 13x13, 100 iterations"},
@@ -707,6 +726,8 @@ def main():
     ap.add_argument("--sizes", type=int, nargs="+", default=list(SIZES))
     ap.add_argument("--rois-5d", type=int, default=50000, help="ROIs of the 5D 17 px figure")
     ap.add_argument("--no-5d", action="store_true")
+    ap.add_argument("--rois-4d", type=int, default=50000, help="ROIs of the 4D 13 px figure")
+    ap.add_argument("--no-4d", action="store_true")
     ap.add_argument("--rois-4pi", type=int, default=100000, help="ROIs of the 4Pi figure")
     ap.add_argument("--no-4pi", action="store_true")
     ap.add_argument("--no-prefilter", action="store_true")

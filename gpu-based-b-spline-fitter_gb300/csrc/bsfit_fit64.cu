@@ -35,6 +35,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 
 #include "bsfit_internal.h"
 
@@ -872,20 +873,41 @@ __global__ void widen_kernel(const float* __restrict__ src, double* __restrict__
   }
 }
 
+// Blocks per SM and SM count of fit64_kernel<MODE> on a device, computed once
+// (the kernel's shared-memory limit is set then), so later launches, including
+// ones captured into a CUDA graph, make no attribute or occupancy calls.
+struct Launch64 {
+  int dev = -1, per_sm = 0, sms = 0;
+};
+std::mutex g_launch64_mu;
+
 template <int MODE>
 cudaError_t launch64(const Fit64Args& a, cudaStream_t stream) {
   using L = F64Layout<MODE>;
   constexpr int WPB = F64Traits<MODE>::WPB;
   const size_t smem = (size_t)L::per_warp * WPB * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(fit64_kernel<MODE>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static Launch64 cache[8];  // per device
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, per_sm = 0;
-  e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fit64_kernel<MODE>, 32 * WPB, smem);
-  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 8) return cudaErrorInvalidDevice;
+  int per_sm = 0, sms = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_launch64_mu);
+    Launch64& c = cache[dev];
+    if (c.dev != dev) {
+      e = cudaFuncSetAttribute(fit64_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sm, fit64_kernel<MODE>, 32 * WPB,
+                                                          smem);
+      if (e != cudaSuccess) return e;
+      c.dev = dev;
+    }
+    per_sm = c.per_sm;
+    sms = c.sms;
+  }
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   const int64_t need = (a.nfits + WPB - 1) / WPB;
   const int64_t cap = (int64_t)sms * per_sm;

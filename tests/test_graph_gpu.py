@@ -68,3 +68,26 @@ def test_captured_batch_replays(bsfit_mod):
     for o, rr in zip(b.outputs, ref):
         for x, y in zip(o, rr):
             assert np.array_equal(x.cpu().numpy(), y, equal_nan=True)
+
+
+def test_captured_fp64_fit_replays(bsfit_mod):
+    """The FP64 kernel too: the warm-up call builds the model's double tables and
+    its launch shape, after which a capture records the launch alone."""
+    import torch
+    from bsfit import workloads as W
+    wl = W.workload_3d(2000, s=13, stream=1044)
+    m = bsfit_mod.Model(6, wl.coeff)
+    r = torch.from_numpy(wl.rois).cuda()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ref = [x.cpu().numpy().copy() for x in m.fit_f64_torch(r, wl.iterations, stream=s)]
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        out = m.fit_f64_torch(r, wl.iterations, stream=s)
+    for x in out:
+        x.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    for a, b in zip(out, ref):
+        assert np.array_equal(a.cpu().numpy(), b, equal_nan=True)

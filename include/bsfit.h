@@ -126,8 +126,11 @@ int32_t bsfit_model_fittype(bsfit_model model);
  * wrappers VC/GPUmleFit_LM/wrapper.cu:256-279 and their kernels
  * VC/GPUmleFit_LM/GPUmleFit_LM_EMCCD.cu:1208-2405). d_rois: nfits ROIs of
  * roi_size^2 floats; d_P / d_CRLB / d_LL: device outputs in the layout above.
- * stream: a cudaStream_t (NULL = legacy default stream). Uses no device memory
- * beyond its arguments.
+ * stream: a cudaStream_t (NULL = legacy default stream). When the ROIs
+ * outnumber the warps resident on the device, the warps claim ROIs from an
+ * 8-byte work counter taken from the stream-ordered pool (cudaMallocAsync /
+ * cudaFreeAsync on `stream`); otherwise it uses no device memory beyond its
+ * arguments. bsfit_batch_fit_device_static allocates nothing at all.
  */
 int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
                      int32_t iterations, float* d_P, float* d_CRLB, float* d_LL, void* stream);

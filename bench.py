@@ -286,7 +286,7 @@ def bench_reference_gpu(groups):
         out = {}
         g13 = next(g for g in groups if g.roi_size == 13)
         w4 = W.workload_4d(20000, sizes=(13,), stream=402)[0]
-        w5 = W.workload_5d(2000, s=17, stream=403)
+        w5 = W.workload_5d(800, s=17, stream=403)  # the reference's 5D kernel: ~100 fits/s
         cases = [("3d_13px", 6, g13.rois[:100000], g13), ("4d_13px", 7, w4.rois, w4),
                  ("5d_17px", 8, w5.rois, w5)]
         for key, ft, rois, wl in cases:
@@ -307,7 +307,7 @@ def bench_reference_gpu(groups):
             stream.synchronize()
             out[key] = len(rois) / (a.elapsed_time(b) / 2 * 1e-3)
         out["workloads"] = ("3D: 100000 ROIs of the step's 13 px group, 30 iterations; 4D: "
-                            "20000 ROIs 13 px, 60 iterations; 5D: 2000 ROIs 17 px, 60 iterations")
+                            "20000 ROIs 13 px, 60 iterations; 5D: 800 ROIs 17 px, 60 iterations")
         out["unit"] = "fits/s"
         out["kernels"] = "GPUmleFit_LM_EMCCD.cu kernel_bsplineMLEFit_*, 64 threads per block"
         return out

@@ -271,9 +271,12 @@ def bench_reference(args):
 
 
 def bench_reference_gpu(groups):
-    """Informational: the reference's own CUDA kernels (one thread per ROI, as
-    its mex launches them) on this GPU, device-resident ROIs, CUDA events; the
-    3D 13 px group of the step, the 4D 13 px and 5D 17 px synthetic models."""
+    """Informational: the reference's own CUDA kernels (one thread per ROI, 64
+    per block, as its mex launches them) on this GPU, device-resident ROIs, CUDA
+    events. Their throughput grows with the ROI count until every SM holds its
+    maximum of 64-thread blocks, so each model gets enough ROIs to fill the GPU:
+    3D 200,000 of the step's 13 px ROIs, 4D 80,000 of 13 px, 5D 38,912 of 17 px
+    (four blocks per SM); one timed launch after a warm-up on a slice."""
     try:
         import torch
         from oracle import ref_gpu
@@ -285,9 +288,9 @@ def bench_reference_gpu(groups):
         stream = torch.cuda.Stream(dev)
         out = {}
         g13 = next(g for g in groups if g.roi_size == 13)
-        w4 = W.workload_4d(20000, sizes=(13,), stream=402)[0]
-        w5 = W.workload_5d(800, s=17, stream=403)  # the reference's 5D kernel: ~100 fits/s
-        cases = [("3d_13px", 6, g13.rois[:100000], g13), ("4d_13px", 7, w4.rois, w4),
+        w4 = W.workload_4d(80000, sizes=(13,), stream=402)[0]
+        w5 = W.workload_5d(38912, s=17, stream=403)
+        cases = [("3d_13px", 6, g13.rois[:200000], g13), ("4d_13px", 7, w4.rois, w4),
                  ("5d_17px", 8, w5.rois, w5)]
         for key, ft, rois, wl in cases:
             d_r = torch.from_numpy(np.ascontiguousarray(rois)).to(dev)
@@ -298,16 +301,17 @@ def bench_reference_gpu(groups):
                 ip = torch.from_numpy(np.asarray(wl.init_p, np.float32)).to(dev)
             dims = list(reversed(wl.coeff.shape))
             with torch.cuda.stream(stream):
-                o = r.fit(ft, d_r, wl.iterations, d_c, dims, d_c3, ip, stream=stream)
+                r.fit(ft, d_r[: max(64, len(rois) // 16)], wl.iterations, d_c, dims, d_c3, ip,
+                      stream=stream)
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a.record(stream)
-                for _ in range(2):
-                    r.fit(ft, d_r, wl.iterations, d_c, dims, d_c3, ip, stream=stream, out=o)
+                r.fit(ft, d_r, wl.iterations, d_c, dims, d_c3, ip, stream=stream)
                 b.record(stream)
             stream.synchronize()
-            out[key] = len(rois) / (a.elapsed_time(b) / 2 * 1e-3)
-        out["workloads"] = ("3D: 100000 ROIs of the step's 13 px group, 30 iterations; 4D: "
-                            "20000 ROIs 13 px, 60 iterations; 5D: 800 ROIs 17 px, 60 iterations")
+            out[key] = len(rois) / (a.elapsed_time(b) * 1e-3)
+        out["workloads"] = ("3D: 200000 ROIs of the step's 13 px group, 30 iterations; 4D: "
+                            "80000 ROIs 13 px, 60 iterations; 5D: 38912 ROIs 17 px, 60 iterations "
+                            "(enough ROIs to fill the GPU with one thread per ROI)")
         out["unit"] = "fits/s"
         out["kernels"] = "GPUmleFit_LM_EMCCD.cu kernel_bsplineMLEFit_*, 64 threads per block"
         return out

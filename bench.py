@@ -661,6 +661,8 @@ def bench_gpu(args):
     if rank != 0:
         return 0
     cpu_n, cpu_t = run_cpu(groups, os.cpu_count() or 1, 0.016)
+    # one core, as the reference's CPU mex runs (a loop over ROIs on one thread)
+    cpu1_n, cpu1_t = run_cpu(groups, 1, 0.002)
     # DRAM traffic of the fitter per step: the ncu capture of the batched
     # kernel on 200k ROIs of the same size mix (summarised under profiles/)
     # measured its bytes against the algorithmic 4 s^2 + 48 B per ROI; the
@@ -704,7 +706,9 @@ def bench_gpu(args):
         "cpu_baseline": {"value": cpu_n / cpu_t, "unit": "fits/s", "cores": os.cpu_count(),
                          "kind": "port",
                          "sample": f"{cpu_n} ROIs (1.6% of each size group), FP32 oracle port of "
-                                   f"the reference CPU fitter, OpenMP over ROIs"},
+                                   f"the reference CPU fitter, OpenMP over ROIs",
+                         "single_core": {"value": cpu1_n / cpu1_t, "unit": "fits/s", "cores": 1,
+                                         "sample": f"{cpu1_n} ROIs (0.2% of each size group)"}},
         "fits_per_s": {"3d_13px": fits_3d13, "4d_13px": fits_4d13,
                        "4d_workload": f"{args.rois_4d} ROIs 13x13, fit type 7, 60 iterations",
                        "5d_17px": fits_5d17,

@@ -124,22 +124,63 @@ __device__ __forceinline__ void warp_sum_array(float (&v)[K]) {
   }
 }
 
-// Reduce-scatter of 32 values over the warp: each lane passes in its 32
-// partial values and gets back the warp total of value number `lane`. Five
-// exchange levels, 31 shuffles (an all-reduce of the same values takes 160).
-__device__ __forceinline__ float reduce_scatter32(float (&v)[32], int lane) {
+// Reduce-scatter of C values (C <= 64) over the warp, five exchange levels
+// o = 16, 8, 4, 2, 1 between lanes l and l ^ o. Of the c values a lane still
+// holds, the first floor(c/2) pair with the next floor(c/2): the lane with bit
+// o set keeps the second of each pair, its partner the first, and an odd last
+// value is kept (and summed) by both. Every value's total is the sum tree of
+// warp_sum (halves differing in bit 16 first, then 8, ...), and floating-point
+// addition is commutative, so every lane holding a value has the same total as
+// a 32-wide butterfly over the value would give; the exchanges number
+// one per value a lane keeps at each level (c -> ceil(c/2)) instead of 31 per
+// 32 values (3D: 20 values, 10 + 5 + 3 + 2 + 1 = 21 exchanges instead of 31).
+// Slot 0 (and slot 1 when C > 32) ends with the value RsSources records.
+template <int C, int O, int N>
+__device__ __forceinline__ void reduce_scatter(float (&v)[N], int lane) {
+  static_assert(C <= N && C <= 64, "reduce_scatter: too many values");
+  if constexpr (O > 0) {
+    constexpr int P = C / 2;
+    const bool up = (lane & O) != 0;
 #pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    const bool up = (lane & o) != 0;
-#pragma unroll
-    for (int i = 0; i < o; ++i) {
-      const float send = up ? v[i] : v[i + o];
-      const float keep = up ? v[i + o] : v[i];
-      v[i] = keep + __shfl_xor_sync(kFull, send, o);
+    for (int i = 0; i < P; ++i) {
+      const float send = up ? v[i] : v[i + P];
+      const float keep = up ? v[i + P] : v[i];
+      v[i] = keep + __shfl_xor_sync(kFull, send, O);
+    }
+    if constexpr ((C & 1) != 0) v[P] = v[2 * P] + __shfl_xor_sync(kFull, v[2 * P], O);
+    reduce_scatter<P + (C & 1), O / 2>(v, lane);
+  }
+}
+
+// Slots a lane holds after reduce_scatter<C, 16> (1 for C <= 32, else 2).
+__host__ __device__ constexpr int rs_slots(int c) {
+  for (int o = 16; o > 0; o >>= 1) c = c / 2 + (c & 1);
+  return c;
+}
+
+// Where each value ends after reduce_scatter<C, 16>: src[x] = 2 * lane + slot
+// of the lowest lane holding value x (the exchange rule above, replayed).
+template <int C>
+struct RsSources {
+  int src[C];
+  __host__ __device__ constexpr RsSources() : src() {
+    for (int x = 0; x < C; ++x) src[x] = -1;
+    for (int lane = 0; lane < 32; ++lane) {
+      int map[64] = {};
+      for (int i = 0; i < C; ++i) map[i] = i;
+      int c = C;
+      for (int o = 16; o > 0; o >>= 1) {
+        const int P = c / 2;
+        const int sh = (lane & o) ? P : 0;
+        for (int i = 0; i < P; ++i) map[i] = map[i + sh];
+        if (c & 1) map[P] = map[2 * P];
+        c = P + (c & 1);
+      }
+      for (int slot = 0; slot < c; ++slot)
+        if (src[map[slot]] < 0) src[map[slot]] = 2 * lane + slot;
     }
   }
-  return v[0];
-}
+};
 
 // Error-free transformations (Knuth two-sum, FMA two-product).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {

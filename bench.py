@@ -216,8 +216,13 @@ def bench_kernel_only(args):
     stream.synchronize()
     n = sum(len(g.rois) for g in groups)
     per_step = 1 if batch is not None else len(groups)
+    # ROI evaluations per step (iterations + 2 per ROI: the initial pass and the
+    # CRLB pass), the unit of an instruction count per evaluation
+    outs = batch.outputs if batch is not None else [o for m, r, o, g in work]
+    evals = sum(float((o[0][5].double() + 2.0).sum().item()) for o in outs) if launches else 0.0
     print(json.dumps({"profile_case": True, "rois": n, "sizes": args.sizes,
-                      "batched": bool(args.batched), "launches": launches * per_step}))
+                      "batched": bool(args.batched), "launches": launches * per_step,
+                      "evaluations_per_step": evals}))
     return 0
 
 

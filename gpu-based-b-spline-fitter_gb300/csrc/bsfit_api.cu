@@ -7,6 +7,7 @@
 // stream-ordered allocator, so repeated calls reuse pooled memory instead of
 // allocating and freeing per call as the reference does.
 #include <algorithm>
+#include <initializer_list>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -528,12 +529,18 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(LL + b, a.LL + b, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, cs_i);
   }
-  // join: c0 waits for c1's last copies
-  if (e == cudaSuccess) e = cudaEventRecord(cs->join, c1);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c0, cs->join, 0);
-  // buffers were allocated on the copy stream: free them on c0 once the copy
-  // stream's work is ordered before it (the chunk events already are)
-  if (cudaEventRecord(cs->join, cp) == cudaSuccess) cudaStreamWaitEvent(c0, cs->join, 0);
+  // Join before the buffers are freed on c0, on the error path too: c0 waits
+  // for c1 (its last copies, or the kernels of chunks already launched there
+  // when a later step failed) and for the copy stream, which allocated the
+  // buffers. Where the join itself cannot be enqueued, the host waits for that
+  // stream instead, so no freed block is still in use by a kernel or copy.
+  for (cudaStream_t other : {c1, cp}) {
+    if (cudaEventRecord(cs->join, other) != cudaSuccess ||
+        cudaStreamWaitEvent(c0, cs->join, 0) != cudaSuccess) {
+      const cudaError_t es = cudaStreamSynchronize(other);
+      if (e == cudaSuccess) e = es;
+    }
+  }
   if (d_rois) cudaFreeAsync(d_rois, c0);
   if (d_out) cudaFreeAsync(d_out, c0);
   if (d_c) cudaFreeAsync(d_c, c0);

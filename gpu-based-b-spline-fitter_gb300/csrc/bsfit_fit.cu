@@ -25,8 +25,11 @@
 //    one refinement step whose residual is computed with error-free FP32
 //    products (float-float), instead of FP64: GB300 issues FP64 at 1/57 of the
 //    FP32 rate and a one-lane FP64 instruction costs as much as a full warp.
-//  * The Fisher information is inverted in FP64 once per fit with the
-//    reference's unpivoted LU (VC/CPUmleFit_LM/MatInvLib.h:17-77).
+//  * The CRLB is the diagonal of the inverse Fisher matrix, computed in FP32
+//    lane-parallel on the Jacobi-scaled matrix D^-1 M D^-1 (unit diagonal) by
+//    Cholesky and the squared columns of L^-1; the reference inverts M itself
+//    in FP32 with an unpivoted LU (VC/CPUmleFit_LM/MatInvLib.h:17-77). The
+//    double-float kernels (bsfit_fitdd.cu) invert it in FP64.
 //
 // Every global read of the coefficient arrays stays inside the array: the
 // knots are clamped exactly as in the reference, and the one coefficient the
@@ -1738,15 +1741,22 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
   FitArgs b = a;
   unsigned long long* claim = nullptr;
   if (need > grid) {
-    if (cudaMallocAsync(reinterpret_cast<void**>(&claim), sizeof(*claim), stream) == cudaSuccess) {
-      if (cudaMemsetAsync(claim, 0, sizeof(*claim), stream) == cudaSuccess) {
+    cudaError_t ea = cudaMallocAsync(reinterpret_cast<void**>(&claim), sizeof(*claim), stream);
+    if (ea == cudaSuccess) {
+      ea = cudaMemsetAsync(claim, 0, sizeof(*claim), stream);
+      if (ea == cudaSuccess) {
         b.claim = claim;
       } else {
         cudaFreeAsync(claim, stream);
         claim = nullptr;
       }
+    } else {
+      claim = nullptr;
     }
-    (void)cudaGetLastError();  // a failed pool allocation leaves the fixed schedule
+    // A failed pool allocation or memset leaves the fixed schedule; only then
+    // is the error it recorded cleared (an error the caller's earlier
+    // asynchronous work left pending is not touched otherwise).
+    if (ea != cudaSuccess) (void)cudaGetLastError();
   }
   kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(b);
   e = cudaGetLastError();

@@ -16,8 +16,12 @@
 //  - two calls whose work overlaps on the GPU (different streams, or host
 //    threads) race on the same counters: serialise them.
 // The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (once per device, with that device current); make that
-// first call before any stream capture. No call allocates or frees memory.
+// cudaGetSymbolAddress (once per device and CUDA context, with that device
+// current); make that first call before any stream capture. The address is
+// kept together with the context it belongs to: after a device reset the
+// primary context is a new one, the array may sit elsewhere, and the next call
+// repeats the look-up (make it, too, before any capture). No call allocates or
+// frees memory.
 #include <cstdint>
 #include <mutex>
 
@@ -25,27 +29,62 @@
 
 namespace {
 
+static_assert(BSFIT_STATIC_MAX_SEGMENTS <= BSFIT_MAX_SEGMENTS,
+              "the static entry forwards to the batched entry, which takes at most "
+              "BSFIT_MAX_SEGMENTS segments");
+
 // Two 64-bit counters (claimed, finished) per segment.
 static __device__ __align__(256) unsigned long long g_static_batch_scratch[2 * BSFIT_STATIC_MAX_SEGMENTS];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {nullptr};
+struct ScratchAddr {
+  void* ctx;   // the CUDA context the address belongs to
+  void* addr;  // device address of g_static_batch_scratch in that context
+};
+ScratchAddr g_scratch[kMaxDevices] = {};
 
-// Device address of the static array on the current device (looked up once per
-// device). Returns a bsfit status.
+// cuCtxGetCurrent through the runtime's driver entry-point query (the library
+// links only the runtime). Null where the query fails: the address is then
+// looked up on every call, which stays correct.
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn ctx_get_current() {
+  static const CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
+
+void* current_ctx() {
+  void* c = nullptr;
+  const CtxGetCurrentFn fn = ctx_get_current();
+  if (!fn || fn(&c) != 0) return nullptr;
+  return c;
+}
+
+// Device address of the static array in the current device's context (looked
+// up once per device and context). Returns a bsfit status.
 int static_scratch(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return BSFIT_E_NO_DEVICE;
   if (dev < 0 || dev >= kMaxDevices) return BSFIT_E_INVALID;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
+  ScratchAddr& c = g_scratch[dev];
+  void* ctx = current_ctx();
+  if (!c.addr || !ctx || ctx != c.ctx) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_static_batch_scratch);
     if (e != cudaSuccess || !p) return BSFIT_E_CUDA;
-    g_scratch_addr[dev] = p;
+    c.addr = p;
+    c.ctx = current_ctx();  // the look-up made the device's context current
   }
-  *out = g_scratch_addr[dev];
+  *out = c.addr;
   return BSFIT_OK;
 }
 

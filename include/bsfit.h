@@ -273,6 +273,8 @@ int bsfit_server_reset_stats(bsfit_server server);
  * counters it uses before its launch, and calls that overlap on the GPU race
  * on them, so serialise such calls. The first call on each device looks the
  * array's address up (cudaGetSymbolAddress); make it before any stream capture.
+ * The address is kept per device and CUDA context: after a device reset the
+ * next call looks it up again (make that call, too, before any capture).
  */
 #define BSFIT_STATIC_MAX_SEGMENTS 48
 int bsfit_batch_fit_device_static(const bsfit_segment* segs, int32_t nseg, void* stream);

@@ -13,7 +13,13 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("BSFIT_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root():
+    """The reference project's root, from the BSFIT_REFERENCE_ROOT environment
+    variable (no default: where it is unset, the reference is not built and the
+    restatement alone, pinned by the committed golden fixtures, is the oracle)."""
+    return os.environ.get("BSFIT_REFERENCE_ROOT") or None
 
 
 def build_oracle(force=False):
@@ -27,17 +33,20 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
-def build_reference(force=False):
-    """Compile the reference CPU fitter when its sources are present."""
-    src = os.path.join(REFERENCE_ROOT, "MultiD_bspline", "visual code",
-                       "CPUmleFit_LM", "CPUmleFit_LM.cpp")
-    if not os.path.exists(src):
-        return None
+def build_reference(force=False, root=None):
+    """Compile the reference CPU fitter from its sources under ``root`` (or
+    BSFIT_REFERENCE_ROOT). Outputs already built are kept unless ``force``."""
     done = all(os.path.exists(os.path.join(REF_DIR, f))
                for f in ("libref_f32.so", "libref_f64.so", "ref_emccd.ptx"))
     if not force and done:
         return REF_DIR
-    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True)
+    root = root or reference_root()
+    if not root:
+        return None
+    src = os.path.join(root, "MultiD_bspline", "visual code", "CPUmleFit_LM", "CPUmleFit_LM.cpp")
+    if not os.path.exists(src):
+        return None
+    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), root], check=True)
     return REF_DIR
 
 

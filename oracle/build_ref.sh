@@ -10,10 +10,14 @@
 # -fno-stack-protector: the 8-parameter solver kernel_luEvaluate5D declares
 # `float y[7]` and writes y[7] (CPUsplineLib.cpp:17-27); without the flag the
 # canary check aborts. The stray element lands in the array's alignment padding.
-# Usage: oracle/build_ref.sh [reference root]   (default /root/reference)
+# Usage: oracle/build_ref.sh <reference root>
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+if [ $# -lt 1 ]; then
+  echo "usage: $0 <reference project root>" >&2
+  exit 2
+fi
+REF="$1"
 SRC="$REF/MultiD_bspline/visual code/CPUmleFit_LM"
 OUT="$HERE/_ref"
 if [ ! -f "$SRC/CPUmleFit_LM.cpp" ]; then

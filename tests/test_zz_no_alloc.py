@@ -5,11 +5,14 @@ fixed-rate acquisition loop, an application owning the GPU's memory pool): the
 work-queue counters live in a fixed array inside the library. This test calls it
 through the C ABI twice in a row and checks each result against the
 caller-scratch entry point, bsfit_batch_fit_device, on the same inputs; the
-second call checks that the counters left behind by the first are cleared. It
-also checks the segment limit of the fixed array. It lives in a file that
-pytest collects last.
+second call checks that the counters left behind by the first are cleared.
+Around each static call it also reads the device's default stream-ordered
+memory pool (used and reserved bytes) and torch's allocator: a call that
+allocated device memory would move them. It also checks the segment limit of
+the fixed array. It lives in a file that pytest collects last.
 """
 import ctypes
+import ctypes.util
 
 import numpy as np
 import pytest
@@ -27,6 +30,22 @@ def _segments(entries, outs, native):
         segs[k].iterations = int(it)
         segs[k].d_P, segs[k].d_CRLB, segs[k].d_LL = P.data_ptr(), C.data_ptr(), L.data_ptr()
     return segs
+
+
+def _pool_bytes(torch):
+    """(used, reserved) bytes of the current device's default memory pool, read
+    through the CUDA runtime's C API (attributes 7 and 5:
+    cudaMemPoolAttrUsedMemCurrent, cudaMemPoolAttrReservedMemCurrent)."""
+    name = ctypes.util.find_library("cudart") or "libcudart.so.13"
+    rt = ctypes.CDLL(name)
+    pool = ctypes.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), torch.cuda.current_device()) == 0
+    out = []
+    for attr in (7, 5):
+        v = ctypes.c_uint64()
+        assert rt.cudaMemPoolGetAttribute(pool, attr, ctypes.byref(v)) == 0
+        out.append(v.value)
+    return tuple(out)
 
 
 def test_static_entry_matches_scratch_entry():
@@ -63,10 +82,14 @@ def test_static_entry_matches_scratch_entry():
     for call in range(2):
         outs = new_outs()
         segs = _segments(entries, outs, _native)
+        torch.cuda.synchronize()
+        pool0, torch0 = _pool_bytes(torch), torch.cuda.memory_allocated()
         st = lib.bsfit_batch_fit_device_static(ctypes.cast(segs, ctypes.c_void_p), len(entries),
                                                stream)
         assert st == 0, lib.bsfit_status_str(st)
         torch.cuda.synchronize()
+        assert _pool_bytes(torch) == pool0, f"call {call}: the memory pool changed"
+        assert torch.cuda.memory_allocated() == torch0, f"call {call}: torch memory changed"
         for (P, C, L), (Pr, Cr, Lr) in zip(outs, ref):
             for a, b in ((P, Pr), (C, Cr), (L, Lr)):
                 a, b = a.cpu().numpy(), b.cpu().numpy()

@@ -619,6 +619,78 @@ def bench_gpu(args):
             b4.record(stream)
         stream.synchronize()
         fits_4pi = w4.n_fits / (a4.elapsed_time(b4) / 2 * 1e-3)
+    def timed(fn, reps=2):
+        # mean ms of reps calls on the bench stream after one untimed call
+        with torch.cuda.stream(stream):
+            fn()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+        stream.synchronize()
+        return a.elapsed_time(b) / reps
+
+    # The colour configuration as stated: 500,000 ROIs of 13 and 15 px (half
+    # each), fit type 7, 60 iterations, through the batched form (one
+    # persistent launch over both sizes).
+    c3_fig = None
+    if not args.no_c3:
+        from bsfit import workloads as W
+        g7 = W.workload_4d(args.rois_c3, sizes=(13, 15), stream=9)
+        m7c = bsfit.Model(7, g7[0].coeff, init_p=g7[0].init_p)
+        b7 = bsfit.Batch([(m7c, torch.from_numpy(g.rois).to(dev), g.iterations) for g in g7])
+        t7 = timed(lambda: b7.run(stream=stream))
+        it7 = float(sum(o[0][6].float().sum().item() for o in b7.outputs) / args.rois_c3)
+        c3_fig = {"fits_per_s": args.rois_c3 / (t7 * 1e-3), "ms": t7, "mean_iterations": it7,
+                  "workload": f"{args.rois_c3} ROIs, 13x13 and 15x15 (half each), fit type 7, "
+                              f"60 iterations, batched (one launch)"}
+        del b7
+    # The 4Pi configuration as stated: 250,000 ROIs of 4 x 16 x 16 px on a
+    # 33 x 33 x 61 x 16 grid periodic in phase, per-channel offsets, 100
+    # iterations, one launch.
+    c4_fig = None
+    if not args.no_c4:
+        from bsfit import workloads as W
+        w4c = W.workload_4pi_c4(args.rois_c4, s=16, stream=10)
+        m4c = bsfit.Model4Pi(w4c.coeff, w4c.extra["phase_shift"])
+        cu = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        r4c, z4c, p4c, d4c = (cu(w4c.rois), cu(w4c.extra["init_z"]), cu(w4c.extra["init_phi"]),
+                              cu(w4c.extra["dT"]))
+        o4c = m4c.fit_torch(r4c, w4c.iterations, z4c, p4c, dT=d4c, stream=stream)
+        t4c = timed(lambda: m4c.fit_torch(r4c, w4c.iterations, z4c, p4c, dT=d4c, stream=stream))
+        stream.synchronize()
+        c4_fig = {"fits_per_s": w4c.n_fits / (t4c * 1e-3), "ms": t4c,
+                  "mean_iterations": float(o4c[0][6].float().mean().item()),
+                  "workload": f"{w4c.n_fits} ROIs of 4 x 16 x 16 px, coefficient grid "
+                              f"{'x'.join(str(d) for d in reversed(w4c.coeff.shape))} (33 x 33 "
+                              f"x 61 lateral / z samples, 16 phases per period, periodic), "
+                              f"per-channel offsets, 100 iterations, one start, one launch"}
+        del r4c
+    # Parity-grade kernels (double-float): 3D 13 px ROIs of the step, the 4D
+    # and 5D figures' workloads.
+    parity_fig = None
+    if not args.no_parity:
+        g13 = next(g for g in groups if g.roi_size == 13)
+        rp = d_rois[groups.index(g13)][:args.rois_parity]
+        mp = models[id(g13.coeff)]
+        tp = timed(lambda: mp.fit_torch(rp, g13.iterations, stream=stream, precision="parity"))
+        parity_fig = {"3d_13px_fits_per_s": rp.shape[0] / (tp * 1e-3),
+                      "3d_workload": f"{rp.shape[0]} ROIs 13x13 of the step, 30 iterations"}
+        if not args.no_4d:
+            n7 = min(args.rois_parity // 2, r7.shape[0])
+            t = timed(lambda: m7.fit_torch(r7[:n7], w7.iterations, stream=stream,
+                                           precision="parity"))
+            parity_fig["4d_13px_fits_per_s"] = n7 / (t * 1e-3)
+            parity_fig["4d_workload"] = f"{n7} ROIs of the 4D figure's workload"
+        if not args.no_5d:
+            n5 = min(args.rois_parity // 10, r5.shape[0])
+            t = timed(lambda: m5.fit_torch(r5[:n5], w5.iterations, stream=stream,
+                                           precision="parity"), reps=1)
+            parity_fig["5d_17px_fits_per_s"] = n5 / (t * 1e-3)
+            parity_fig["5d_workload"] = f"{n5} ROIs of the 5D figure's workload"
+        parity_fig["kernel"] = ("fitdd_kernel<6|7|8>: the reference method in double-float on "
+                                "the FP32 pipe, Fisher inverse in FP64")
     # FP64 reference-precision kernel (bit-identical to the FP64 oracle) on
     # 3D 13 px ROIs of the step's workload.
     fp64_fig = None
@@ -720,6 +792,9 @@ def bench_gpu(args):
                        "5d_workload": f"{args.rois_5d} ROIs 17x17, fit type 8, 60 iterations",
                        "4pi_13px": fits_4pi,
                        "4pi_workload": f"{args.rois_4pi} ROIs of 4 channels 13x13, 100 iterations"},
+        "config_3_colour": c3_fig,
+        "config_4_4pi": c4_fig,
+        "parity_precision": parity_fig,
         "reference_precision": fp64_fig,
         "prefilter": prefilter_fig,
         "frontend": frontend_fig,
@@ -750,6 +825,13 @@ def main():
     ap.add_argument("--no-4d", action="store_true")
     ap.add_argument("--rois-4pi", type=int, default=100000, help="ROIs of the 4Pi figure")
     ap.add_argument("--no-4pi", action="store_true")
+    ap.add_argument("--rois-c3", type=int, default=500000, help="ROIs of the colour configuration")
+    ap.add_argument("--no-c3", action="store_true")
+    ap.add_argument("--rois-c4", type=int, default=250000, help="ROIs of the 4Pi configuration")
+    ap.add_argument("--no-c4", action="store_true")
+    ap.add_argument("--rois-parity", type=int, default=100000,
+                    help="3D ROIs of the parity-grade figure (4D: half, 5D: a tenth)")
+    ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-prefilter", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-ref-gpu", action="store_true",

@@ -35,7 +35,10 @@ def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, s
     """Drop-in for the reference mex (fit types 6, 7, 8); raises BsfitError.
 
     Returns (P, CRLB, LL) shaped (N, NV + 1), (N, NV), (N,): views of the C
-    ABI's column-major outputs (no copy). out=(P, CRLB, LL) passes caller-owned
+    ABI's column-major outputs (no copy). precision="parity" runs the
+    double-float kernels (bsfit_GPUmleFit_LM_multiD_parity): float32 outputs
+    that follow the reference's FP64 trajectory as closely as a second FP64
+    build of it. out=(P, CRLB, LL) passes caller-owned
     buffers in the C ABI's layout ((NV + 1, N), (NV, N), (N,)), which are
     filled and returned as the same views, as a host application calling the C
     ABI directly would reuse its buffers. precision="f64" runs the FP64
@@ -54,9 +57,9 @@ def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, s
     c3 = _f32(coeff3) if coeff3 is not None else None
     ip = _f32(np.atleast_1d(initP)) if initP is not None else None
     vm = _f32(np.atleast_1d(varmap)) if varmap is not None else None
-    if precision not in ("f32", "f64"):
-        raise ValueError("precision must be 'f32' or 'f64'")
-    dt = np.float32 if precision == "f32" else np.float64
+    if precision not in ("f32", "f64", "parity"):
+        raise ValueError("precision must be 'f32', 'parity' or 'f64'")
+    dt = np.float64 if precision == "f64" else np.float32
     if out is None:
         P = np.empty((max(nv, 1) + 1, n), dt)
         C = np.empty((max(nv, 1), n), dt)
@@ -66,8 +69,9 @@ def GPUmleFit_LM_multiD(imstack, fittype, iterations=50, coeff=None, varmap=0, s
         assert P.shape == (nv + 1, n) and C.shape == (nv, n) and L.shape == (n,)
         assert all(x.dtype == dt and x.flags.c_contiguous for x in (P, C, L))
     ptr = lambda a: a.ctypes.data_as(_fp) if a is not None else None  # noqa: E731
-    optr = (lambda a: a.ctypes.data_as(_fp)) if precision == "f32" else (lambda a: a.ctypes.data)
-    fn = lib.bsfit_GPUmleFit_LM_multiD if precision == "f32" else lib.bsfit_GPUmleFit_LM_multiD_f64
+    optr = (lambda a: a.ctypes.data) if precision == "f64" else (lambda a: a.ctypes.data_as(_fp))
+    fn = {"f32": lib.bsfit_GPUmleFit_LM_multiD, "parity": lib.bsfit_GPUmleFit_LM_multiD_parity,
+          "f64": lib.bsfit_GPUmleFit_LM_multiD_f64}[precision]
     st = fn(
         ptr(im), s1, s2, n, fittype, int(iterations),
         ptr(c), c.ndim if c is not None else 0, _dims(c) if c is not None else None,
@@ -111,15 +115,25 @@ class Model:
         check(st, "bsfit_model_create")
         self._h = h
 
-    def fit_device(self, d_rois, roi_size, nfits, iterations, d_P, d_CRLB, d_LL, stream=0):
-        """Asynchronous fit with raw device pointers (ints) on a CUDA stream."""
-        st = _native.lib().bsfit_fit_device(self._h, d_rois, roi_size, nfits, iterations,
-                                            d_P, d_CRLB, d_LL, stream)
+    def fit_device(self, d_rois, roi_size, nfits, iterations, d_P, d_CRLB, d_LL, stream=0,
+                   precision="f32", exact_steps=-1):
+        """Asynchronous fit with raw device pointers (ints) on a CUDA stream;
+        precision="parity" runs the double-float kernels (exact_steps: leading
+        LM steps in the FP64 reference order, -1 the default per fit type)."""
+        lib = _native.lib()
+        if precision == "parity":
+            st = lib.bsfit_fit_parity_steps_device(self._h, d_rois, roi_size, nfits, iterations,
+                                                   int(exact_steps), d_P, d_CRLB, d_LL, stream)
+            check(st, "bsfit_fit_parity_steps_device")
+            return
+        st = lib.bsfit_fit_device(self._h, d_rois, roi_size, nfits, iterations, d_P, d_CRLB,
+                                  d_LL, stream)
         check(st, "bsfit_fit_device")
 
-    def fit_torch(self, rois, iterations, out=None, stream=None):
+    def fit_torch(self, rois, iterations, out=None, stream=None, precision="f32", exact_steps=-1):
         """Fit a CUDA float32 tensor (N, s, s); returns (P, CRLB, LL) tensors in
-        the reference's column-major layout: P (NV+1, N), CRLB (NV, N), LL (N)."""
+        the reference's column-major layout: P (NV+1, N), CRLB (NV, N), LL (N).
+        precision="parity" runs the double-float kernels."""
         import torch
         assert rois.is_cuda and rois.dtype == torch.float32 and rois.is_contiguous()
         n, s = rois.shape[0], rois.shape[-1]
@@ -131,7 +145,7 @@ class Model:
             P, C, L = out
         st = stream if stream is not None else torch.cuda.current_stream(rois.device)
         self.fit_device(rois.data_ptr(), s, n, int(iterations), P.data_ptr(), C.data_ptr(),
-                        L.data_ptr(), st.cuda_stream)
+                        L.data_ptr(), st.cuda_stream, precision=precision, exact_steps=exact_steps)
         return P, C, L
 
     def fit_scmos_torch(self, rois, var, iterations, stream=None):
@@ -210,17 +224,20 @@ class Model:
                                                T.data_ptr(), tm, st.cuda_stream), "bsfit_trace_device")
         return P, C, L, T
 
-    def eval_torch(self, rois, theta, fisher=False, stream=None):
-        """One evaluation per ROI at theta (tensor (NV, N)); returns (N, 1+NV+NH)."""
+    def eval_torch(self, rois, theta, fisher=False, stream=None, precision="f32"):
+        """One evaluation per ROI at theta (tensor (NV, N)); returns (N, 1+NV+NH),
+        float32, or float64 from the double-float evaluation (precision="parity")."""
         import torch
         n, s = rois.shape[0], rois.shape[-1]
         nh = self.nv * (self.nv + 1) // 2
-        out = torch.empty((n, 1 + self.nv + nh), device=rois.device, dtype=torch.float32)
+        dt = torch.float64 if precision == "parity" else torch.float32
+        out = torch.empty((n, 1 + self.nv + nh), device=rois.device, dtype=dt)
         theta = theta.contiguous()
         st = stream if stream is not None else torch.cuda.current_stream(rois.device)
-        check(_native.lib().bsfit_eval_device(self._h, rois.data_ptr(), s, n, theta.data_ptr(),
-                                              int(bool(fisher)), out.data_ptr(), st.cuda_stream),
-              "bsfit_eval_device")
+        name = "bsfit_eval_parity_device" if precision == "parity" else "bsfit_eval_device"
+        check(getattr(_native.lib(), name)(self._h, rois.data_ptr(), s, n, theta.data_ptr(),
+                                           int(bool(fisher)), out.data_ptr(), st.cuda_stream),
+              name)
         return out
 
     def close(self):

@@ -22,6 +22,31 @@ SIGNATURES = {
         _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
         _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int64,
         _fp, ctypes.c_int32, _i64p, _fp, _fp, _fp]),
+    "bsfit_GPUmleFit_LM_multiD_parity": (ctypes.c_int, [
+        _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+        _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int64,
+        _fp, ctypes.c_int32, _i64p, _fp, _fp, _fp]),
+    "bsfit_eval_parity_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+        ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
+    "bsfit_tune_num_variants": (ctypes.c_int, [ctypes.c_int32]),
+    "bsfit_tune_min_blocks": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
+    "bsfit_tune_set": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                      ctypes.c_int32]),
+    "bsfit_tune_get": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64,
+                                      ctypes.POINTER(ctypes.c_int32),
+                                      ctypes.POINTER(ctypes.c_int32)]),
+    "bsfit_autotune_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+        ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+    "bsfit_fit_parity_steps_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+        ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "bsfit_fit_parity_device": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "bsfit_GPUmleFit_LM_multiD_f64": (ctypes.c_int, [
         _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
         _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int64,

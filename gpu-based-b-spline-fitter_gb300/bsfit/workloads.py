@@ -399,3 +399,96 @@ def workload_4pi(n=100_000, s=13, iterations=100, stream=6, start_phase=2 * np.p
     extra = dict(dT=dT, init_z=init_z, init_phi=init_phi,
                  phase_shift=(PHASE_SHIFTS / PHI_STEP).astype(np.float32))
     return Workload(f"4pi_{s}px", 9, iterations, coeff4pi(), rois, truth, extra=extra)
+
+
+# ---------------------------------------------------------------------------
+# 4Pi workload of the benchmark's stated 4Pi configuration: four channels
+# I_c = G(x, y, z) [1 + 0.8 cos(psi + c pi/2)] with the interference phase
+# psi = 2 pi z / 260 nm + phi, a per-ROI phase offset phi; 16 px ROIs; the
+# coefficient grid samples 33 x 33 lateral, 61 z (-600..600 nm) and 16 phases
+# per period, periodic in phase; per-channel lateral offsets uniform within
+# +-0.5 px; photons split evenly over the channels.
+
+N_PHI_C4 = 16
+PHI_STEP_C4 = 2 * np.pi / N_PHI_C4
+PHASE_PERIOD_NM_C4 = 260.0
+C4_LAT = 33
+
+
+def _c4_centre(s, n_lat=C4_LAT):
+    """Sample index of the PSF centre for s px ROIs on an n_lat-sample lateral
+    grid: pixel jj of an emitter at x sits at knot (s + 1) // 2 - x + jj +
+    (nX - s) / 2 with nX = n_lat - 1 (CPUmleFit_LM.cpp:2512-2519), and sample j
+    at knot j + 1."""
+    return (s + 1) // 2 + (n_lat - 1 - s) / 2.0 - 1.0
+
+
+def psf4pi_c4_samples(s=16, n_lat=C4_LAT, z_lo=-600.0, z_hi=600.0, n_phi=N_PHI_C4):
+    """(W, Z, X, Y): the astigmatic PSF times 1 + 0.8 cos(phase) at n_phi
+    phases over one period."""
+    nz = int(round((z_hi - z_lo) / Z_STEP_NM)) + 1
+    z = z_lo + Z_STEP_NM * np.arange(nz)
+    c = _c4_centre(s, n_lat)
+    sx, sy = astig_sigmas(z, 1.3)
+    base = _int_gauss(np.full(nz, c), sx, n_lat)[:, :, None] * _int_gauss(np.full(nz, c), sy, n_lat)[:, None, :]
+    ph = PHI_STEP_C4 * np.arange(n_phi)
+    return base[None] * (1.0 + 0.8 * np.cos(ph))[:, None, None, None], z
+
+
+def coeff4pi_c4(s=16, n_lat=C4_LAT, n_phi=N_PHI_C4):
+    """Coefficients (W, Z, X, Y): mirror prefilter and pad along Z, X, Y; the
+    periodic interpolating spline along the phase, laid out for the fitter's
+    wrap (period W - 4 knots, phase position w in [1, 1 + period), sample j at
+    w = j + 1): plane m holds the periodic coefficient (m - 1) mod n_phi, for
+    m = 0 .. n_phi + 3."""
+    key = ("4pi_c4", s, n_lat, n_phi)
+    if key not in _COEFF_CACHE:
+        smp, _ = psf4pi_c4_samples(s, n_lat, n_phi=n_phi)
+        c = smp
+        for ax in (1, 2, 3):
+            c = prefilter.filter_axis(c, ax)
+        c = prefilter.filter_axis_periodic(c, 0)
+        c = prefilter.mirror_pad(c, axes=(1, 2, 3))
+        m = np.arange(n_phi + 4)
+        c = np.take(c, (m - 1) % n_phi, axis=0)
+        _COEFF_CACHE[key] = np.ascontiguousarray(c.astype(np.float32))
+    return _COEFF_CACHE[key]
+
+
+def workload_4pi_c4(n=250_000, s=16, iterations=100, stream=7, z_range=500.0, chunk=65536):
+    """The stated 4Pi configuration: n ROIs of 4 x s x s; x, y within +-1 px of
+    the centre, z uniform within +-z_range nm, phase offset uniform on [0, 2 pi),
+    total photons log-uniform 2000-10000 split evenly over the channels,
+    background uniform 5-20 per pixel and channel, per-channel lateral offsets
+    uniform within +-0.5 px (passed to the fit as dT). One start: z mid-range,
+    phase at the first knot."""
+    rng = _rng(stream)
+    cx = (s - 1) / 2.0
+    x = cx + rng.uniform(-1.0, 1.0, n)
+    y = cx + rng.uniform(-1.0, 1.0, n)
+    z = rng.uniform(-z_range, z_range, n)
+    phi = rng.uniform(0.0, 2 * np.pi, n)
+    psi = np.mod(2 * np.pi * z / PHASE_PERIOD_NM_C4 + phi, 2 * np.pi)
+    n_tot = np.exp(rng.uniform(math.log(2000.0), math.log(10000.0), n))
+    photons = n_tot / 4.0
+    bg = rng.uniform(5.0, 20.0, n)
+    dT = np.zeros((n, 4, 6), np.float32)
+    dT[:, :, 0] = rng.uniform(-0.5, 0.5, (n, 4))
+    dT[:, :, 1] = rng.uniform(-0.5, 0.5, (n, 4))
+    sx, sy = astig_sigmas(z, 1.3)
+    rois = np.empty((4, n, s, s), np.float32)
+    for c in range(4):
+        for b in range(0, n, chunk):
+            e = min(n, b + chunk)
+            gx = _int_gauss(x[b:e] + dT[b:e, c, 0], sx[b:e], s)
+            gy = _int_gauss(y[b:e] + dT[b:e, c, 1], sy[b:e], s)
+            mod = 1.0 + 0.8 * np.cos(psi[b:e] + c * 0.5 * np.pi)
+            model = bg[b:e, None, None] + (photons[b:e] * mod)[:, None, None] * gx[:, :, None] * gy[:, None, :]
+            rois[c, b:e] = rng.poisson(model)
+    truth = dict(x=x, y=y, z_nm=z, z=z_to_param(z), phi=phi, psi=psi,
+                 w=psi / PHI_STEP_C4 + 1.0, N=photons, bg=bg)
+    init_z = np.full(n, z_to_param(0.0), np.float32)
+    init_phi = np.full(n, 1.0, np.float32)
+    shifts = (np.arange(4) * 0.5 * np.pi / PHI_STEP_C4).astype(np.float32)
+    extra = dict(dT=dT, init_z=init_z, init_phi=init_phi, phase_shift=shifts)
+    return Workload(f"4pi_c4_{s}px", 9, iterations, coeff4pi_c4(s), rois, truth, extra=extra)

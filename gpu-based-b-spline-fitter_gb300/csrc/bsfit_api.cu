@@ -324,6 +324,24 @@ int bsfit_eval_device(bsfit_model model, const float* d_rois, int64_t roi_size, 
   return cuda_status(bsfit::launch_eval(a, d_theta, d_out, fisher, (cudaStream_t)stream));
 }
 
+int bsfit_eval_parity_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                             int64_t nfits, const float* d_theta, int32_t fisher, double* d_out,
+                             void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  if (model->dev.fittype == bsfit::kFit4Pi) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_theta || !d_out) return BSFIT_E_INVALID;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  return cuda_status(bsfit::launch_evaldd(a, d_theta, d_out, fisher, (cudaStream_t)stream));
+}
+
 int64_t bsfit_batch_scratch_bytes(int32_t nseg) {
   if (nseg < 0) return 0;
   return (((int64_t)nseg * 2 * 8) + 255) / 256 * 256;
@@ -427,15 +445,16 @@ int bsfit_batch_fit_multistart_device(const bsfit_segment* segs, const bsfit_sta
   return batch_fit(segs, starts, nseg, d_scratch, scratch_bytes, stream);
 }
 
-int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t roi_size2,
-                              int64_t nfits, int32_t fittype, int32_t iterations,
-                              const float* coeff, int32_t coeff_ndim, const int64_t* coeff_dims,
-                              const float* varmap, int64_t varmap_numel, int32_t silent,
-                              const float* init_p, int64_t init_p_numel, const float* coeff3,
-                              int32_t coeff3_ndim, const int64_t* coeff3_dims, float* P,
-                              float* CRLB, float* LL) {
-  (void)varmap;
-  (void)varmap_numel;  // ignored for fit types 6-8, as in the reference
+}  // extern "C"
+
+namespace {
+
+// The synchronous drop-in call of the FP32 kernels (bsfit_GPUmleFit_LM_multiD).
+int multid_call(const float* imstack, int64_t roi_size, int64_t roi_size2, int64_t nfits,
+                int32_t fittype, int32_t iterations, const float* coeff, int32_t coeff_ndim,
+                const int64_t* coeff_dims, int32_t silent, const float* init_p,
+                int64_t init_p_numel, const float* coeff3, int32_t coeff3_ndim,
+                const int64_t* coeff3_dims, float* P, float* CRLB, float* LL) {
   int st = call_checks(imstack, roi_size, roi_size2, nfits, fittype, P && CRLB && LL);
   if (st) return st;
   const int nv = num_params(fittype);
@@ -548,6 +567,24 @@ int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t ro
   cudaError_t e2 = cudaStreamSynchronize(c0);
   if (e == cudaSuccess) e = e2;
   return cuda_status(e);
+}
+
+}  // namespace
+
+extern "C" {
+
+int bsfit_GPUmleFit_LM_multiD(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                              int64_t nfits, int32_t fittype, int32_t iterations,
+                              const float* coeff, int32_t coeff_ndim, const int64_t* coeff_dims,
+                              const float* varmap, int64_t varmap_numel, int32_t silent,
+                              const float* init_p, int64_t init_p_numel, const float* coeff3,
+                              int32_t coeff3_ndim, const int64_t* coeff3_dims, float* P,
+                              float* CRLB, float* LL) {
+  (void)varmap;
+  (void)varmap_numel;  // ignored for fit types 6-8, as in the reference
+  return multid_call(imstack, roi_size, roi_size2, nfits, fittype, iterations, coeff, coeff_ndim,
+                     coeff_dims, silent, init_p, init_p_numel, coeff3, coeff3_ndim, coeff3_dims, P,
+                     CRLB, LL);
 }
 
 // ---------------------------------------------------------------------------
@@ -896,6 +933,150 @@ int bsfit_fit_f64_device(bsfit_model model, const float* d_rois, const float* d_
   return cuda_status(bsfit::launch_fit64(a, st));
 }
 
+}  // extern "C"
+
+namespace {
+
+// Leading LM steps of the parity-grade fit taken by the FP64 reference-order
+// kernel, per fit type (6, 7, 8): fit type 7's initial Hessian is exactly
+// singular (its initial pass copies dudt[4] into dudt[5], CPUmleFit_LM.cpp:2893),
+// so its first step is set by the rounding of the reference's double sums and
+// is taken in that arithmetic.
+int default_exact_steps(int fittype) { return fittype == 7 ? 1 : 0; }
+
+int parity_fit(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+               int32_t iterations, int32_t exact_steps, float* d_P, float* d_CRLB, float* d_LL,
+               void* stream) {
+  if (!model) return BSFIT_E_INVALID;
+  const int ft = model->dev.fittype;
+  if (ft != 6 && ft != 7 && ft != 8) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 0 || exact_steps < -1) return BSFIT_E_INVALID;
+  if (nfits == 0) return BSFIT_OK;
+  if (!d_rois || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  if (exact_steps < 0) exact_steps = default_exact_steps(ft);
+  cudaStream_t st = (cudaStream_t)stream;
+  FitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = model->dev;
+  a.rois = d_rois;
+  a.s = (int)roi_size;
+  a.nfits = nfits;
+  a.iterations = iterations;
+  a.P = d_P;
+  a.CRLB = d_CRLB;
+  a.LL = d_LL;
+  a.out_n = nfits;
+  a.flags = bsfit::FLAG_PARITY;
+  if (exact_steps == 0 || iterations <= 0)
+    return cuda_status(bsfit::launch_fit(a, st));
+  // FP64 reference-order pre-pass: the initial evaluation and the first
+  // exact_steps LM steps of every ROI, handed over through a pooled buffer.
+  const int rc = ensure_f64_tables(model, st);
+  if (rc != BSFIT_OK) return rc;
+  const ModelDev& m = model->dev;
+  double* handoff = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&handoff),
+                                  (size_t)nfits * bsfit::kHandoffStride * sizeof(double), st);
+  if (e != cudaSuccess) return cuda_status(e);
+  bsfit::Fit64Args f;
+  std::memset(&f, 0, sizeof(f));
+  f.m = m;
+  f.c = model->d_coeff64;
+  f.c3 = model->d_coeff3_64;
+  f.total = 1;
+  for (int i = 0; i < 5; ++i) f.total *= m.cd[i];
+  f.total3 = (int64_t)m.cd[0] * m.cd[1] * m.cd[2];
+  f.rois = d_rois;
+  f.s = (int)roi_size;
+  f.nfits = nfits;
+  f.iterations = iterations;
+  f.handoff = handoff;
+  f.handoff_iters = exact_steps;
+  e = bsfit::launch_fit64(f, st);
+  if (e == cudaSuccess) {
+    a.handoff = handoff;
+    e = bsfit::launch_fit(a, st);
+  }
+  cudaFreeAsync(handoff, st);
+  return cuda_status(e);
+}
+
+}  // namespace
+
+extern "C" {
+
+int bsfit_fit_parity_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                            int64_t nfits, int32_t iterations, float* d_P, float* d_CRLB,
+                            float* d_LL, void* stream) {
+  return parity_fit(model, d_rois, roi_size, nfits, iterations, -1, d_P, d_CRLB, d_LL, stream);
+}
+
+int bsfit_fit_parity_steps_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                                  int64_t nfits, int32_t iterations, int32_t exact_steps,
+                                  float* d_P, float* d_CRLB, float* d_LL, void* stream) {
+  return parity_fit(model, d_rois, roi_size, nfits, iterations, exact_steps, d_P, d_CRLB, d_LL,
+                    stream);
+}
+
+// The drop-in call of the parity-grade fit: the arguments and checks of
+// bsfit_GPUmleFit_LM_multiD, float outputs from bsfit_fit_parity_device.
+int bsfit_GPUmleFit_LM_multiD_parity(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                                     int64_t nfits, int32_t fittype, int32_t iterations,
+                                     const float* coeff, int32_t coeff_ndim,
+                                     const int64_t* coeff_dims, const float* varmap,
+                                     int64_t varmap_numel, int32_t silent, const float* init_p,
+                                     int64_t init_p_numel, const float* coeff3,
+                                     int32_t coeff3_ndim, const int64_t* coeff3_dims, float* P,
+                                     float* CRLB, float* LL) {
+  (void)varmap;
+  (void)varmap_numel;
+  int st = call_checks(imstack, roi_size, roi_size2, nfits, fittype, P && CRLB && LL);
+  if (st) return st;
+  const int nv = num_params(fittype);
+  if (!silent) {
+    std::printf("subregion size: %lld fittype: %d\n", (long long)roi_size, fittype);
+    std::printf("Number of fits: %lld no padding\n", (long long)nfits);
+  }
+  bsfit_model model = nullptr;
+  st = bsfit_model_create(fittype, coeff, coeff_ndim, coeff_dims, coeff3, coeff3_ndim,
+                          coeff3_dims, init_p, init_p_numel, &model);
+  if (st) return st;
+  if (nfits == 0) return bsfit_model_release(model);
+  CallStreams* cs = call_streams();
+  if (!cs) {
+    bsfit_model_release(model);
+    return BSFIT_E_CUDA;
+  }
+  cudaStream_t cst = cs->comp[0];
+  const size_t s2 = (size_t)roi_size * roi_size;
+  const size_t in_bytes = (size_t)nfits * s2 * sizeof(float);
+  const size_t nout = (size_t)nfits * (2 * nv + 2);
+  float* d_rois = nullptr;
+  float* d_out = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_rois, in_bytes, cst);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_out, nout * sizeof(float), cst);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rois, imstack, in_bytes, cudaMemcpyHostToDevice, cst);
+  int rc = BSFIT_OK;
+  float* dP = d_out;
+  float* dC = d_out + (size_t)nfits * (nv + 1);
+  float* dL = dC + (size_t)nfits * nv;
+  if (e == cudaSuccess) rc = parity_fit(model, d_rois, roi_size, nfits, iterations, -1, dP, dC, dL, cst);
+  if (e == cudaSuccess && rc == BSFIT_OK)
+    e = cudaMemcpyAsync(P, dP, (size_t)nfits * (nv + 1) * sizeof(float), cudaMemcpyDeviceToHost, cst);
+  if (e == cudaSuccess && rc == BSFIT_OK)
+    e = cudaMemcpyAsync(CRLB, dC, (size_t)nfits * nv * sizeof(float), cudaMemcpyDeviceToHost, cst);
+  if (e == cudaSuccess && rc == BSFIT_OK)
+    e = cudaMemcpyAsync(LL, dL, (size_t)nfits * sizeof(float), cudaMemcpyDeviceToHost, cst);
+  if (d_rois) cudaFreeAsync(d_rois, cst);
+  if (d_out) cudaFreeAsync(d_out, cst);
+  cudaError_t e2 = cudaStreamSynchronize(cst);
+  bsfit_model_release(model);
+  if (rc != BSFIT_OK) return rc;
+  if (e == cudaSuccess) e = e2;
+  return cuda_status(e);
+}
+
 // The drop-in call with double results from the FP64 reference-precision
 // kernel: same arguments and checks as bsfit_GPUmleFit_LM_multiD (varmap
 // ignored likewise), double outputs in the same column-major layout.
@@ -992,6 +1173,106 @@ int bsfit_fit4pi_f64_device(bsfit_model model, const float* d_rois, int64_t roi_
   a.z0 = d_initZ;
   a.w0 = d_initPhi;
   return cuda_status(bsfit::launch_fit64(a, st));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner (bsfit_tune.cu holds the configuration table and the kernel
+// variants).
+
+extern "C" {
+
+int bsfit_tune_num_variants(int32_t fittype) { return bsfit::tune_num_variants(fittype); }
+
+int bsfit_tune_min_blocks(int32_t fittype, int32_t variant) {
+  return bsfit::tune_min_blocks(fittype, variant);
+}
+
+int bsfit_tune_set(int32_t fittype, int64_t roi_size, int32_t variant, int32_t warps_per_block) {
+  if (num_params(fittype) == 0) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return BSFIT_E_NO_DEVICE;
+  if (variant < 0) {
+    bsfit::tune_clear(fittype, (int)roi_size, dev);
+    return BSFIT_OK;
+  }
+  if (!bsfit::tune_store(fittype, (int)roi_size, dev, bsfit::TuneConfig{variant, warps_per_block}))
+    return BSFIT_E_INVALID;
+  return BSFIT_OK;
+}
+
+int bsfit_tune_get(int32_t fittype, int64_t roi_size, int32_t* variant, int32_t* warps_per_block) {
+  if (!variant || !warps_per_block) return BSFIT_E_INVALID;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return BSFIT_E_NO_DEVICE;
+  bsfit::TuneConfig c{0, 0};
+  const bool found = bsfit::tune_lookup(fittype, (int)roi_size, dev, &c);
+  *variant = found ? c.variant : -1;
+  *warps_per_block = found ? c.wpb : 0;
+  return BSFIT_OK;
+}
+
+int bsfit_autotune_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                          int32_t iterations, float* d_P, float* d_CRLB, float* d_LL, int32_t reps,
+                          int32_t* best_variant, int32_t* best_wpb, double* best_ms,
+                          double* all_ms, void* stream) {
+  if (!model || !best_variant || !best_wpb) return BSFIT_E_INVALID;
+  const int ft = model->dev.fittype;
+  if (ft != 6 && ft != 7 && ft != 8) return BSFIT_E_UNSUPPORTED_FITTYPE;
+  if (roi_size < 1 || roi_size > kMaxRoi) return BSFIT_E_SUBREGION_SIZE;
+  if (nfits < 1 || reps < 1 || !d_rois || !d_P || !d_CRLB || !d_LL) return BSFIT_E_INVALID;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return BSFIT_E_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return cuda_status(e);
+  }
+  const int nv = bsfit::tune_num_variants(ft);
+  const int wpbs[3] = {4, 2, 1};
+  double best = -1.0;
+  bsfit::TuneConfig bc{0, 0};
+  int rc = BSFIT_OK;
+  for (int v = 0; v < nv && rc == BSFIT_OK; ++v)
+    for (int w = 0; w < 3 && rc == BSFIT_OK; ++w) {
+      bsfit::tune_store(ft, (int)roi_size, dev, bsfit::TuneConfig{v, wpbs[w]});
+      double ms = -1.0;  // infeasible (shared memory or occupancy)
+      int r = bsfit_fit_device(model, d_rois, roi_size, nfits, iterations, d_P, d_CRLB, d_LL, st);
+      if (r == BSFIT_OK) {
+        cudaEventRecord(e0, st);
+        for (int k = 0; k < reps && r == BSFIT_OK; ++k)
+          r = bsfit_fit_device(model, d_rois, roi_size, nfits, iterations, d_P, d_CRLB, d_LL, st);
+        cudaEventRecord(e1, st);
+        e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) rc = cuda_status(e);
+        float t = 0.0f;
+        if (r == BSFIT_OK && e == cudaSuccess && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess)
+          ms = (double)t / reps;
+      } else if (r != BSFIT_E_CUDA) {
+        rc = r;
+      }
+      if (all_ms) all_ms[v * 3 + w] = ms;
+      if (ms > 0.0 && (best < 0.0 || ms < best)) {
+        best = ms;
+        bc = bsfit::TuneConfig{v, wpbs[w]};
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != BSFIT_OK || best < 0.0) {
+    bsfit::tune_clear(ft, (int)roi_size, dev);
+    return rc != BSFIT_OK ? rc : BSFIT_E_CUDA;
+  }
+  bsfit::tune_store(ft, (int)roi_size, dev, bc);
+  *best_variant = bc.variant;
+  *best_wpb = bc.wpb;
+  if (best_ms) *best_ms = best;
+  return BSFIT_OK;
 }
 
 }  // extern "C"

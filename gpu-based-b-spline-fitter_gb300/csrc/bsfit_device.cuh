@@ -6,6 +6,7 @@
 
 #include <climits>
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace bsfit {
@@ -181,6 +182,43 @@ struct RsSources {
     }
   }
 };
+
+// Where lane l < NV finds gradient entry l (grad) and Hessian entry (l, k)
+// (row[k]) after reduce_scatter of the K = NV + NV(NV+1)/2 sums: B bits per
+// lane, the source lane (one slot per lane), or 2 * lane + slot (two slots).
+template <int NV, int K>
+struct GatherCodes {
+  static constexpr int SLOTS = rs_slots(K);
+  static constexpr int B = SLOTS > 1 ? 6 : 5;
+  using Code = typename std::conditional<NV * B <= 32, unsigned, unsigned long long>::type;
+  Code grad;
+  Code row[NV];
+  __host__ __device__ constexpr GatherCodes() : grad(0), row() {
+    const RsSources<K> rs{};
+    const int div = SLOTS > 1 ? 1 : 2;  // one slot: the lane alone
+    for (int l = 0; l < NV; ++l) grad |= (Code)(rs.src[l] / div) << (B * l);
+    for (int k = 0; k < NV; ++k)
+      for (int l = 0; l < NV; ++l) {
+        const int lo = l < k ? l : k, hi = l < k ? k : l;
+        const int x = NV + lo * NV - (lo * (lo - 1)) / 2 + (hi - lo);
+        row[k] |= (Code)(rs.src[x] / div) << (B * l);
+      }
+  }
+};
+
+// This lane's value (its field of codes, starting at bit sh) from the lane
+// that holds it.
+template <int SLOTS, typename Code>
+__device__ __forceinline__ float rs_gather(float t0, float t1, Code codes, int sh) {
+  if constexpr (SLOTS > 1) {
+    const int code = (int)((codes >> sh) & 63u);
+    const float a0 = __shfl_sync(kFull, t0, code >> 1);
+    const float a1 = __shfl_sync(kFull, t1, code >> 1);
+    return (code & 1) ? a1 : a0;
+  } else {
+    return __shfl_sync(kFull, t0, (int)((codes >> sh) & 31u));
+  }
+}
 
 // Error-free transformations (Knuth two-sum, FMA two-product).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {

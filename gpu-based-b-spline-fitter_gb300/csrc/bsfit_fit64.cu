@@ -823,6 +823,63 @@ __global__ void __launch_bounds__(32 * F64Traits<MODE>::WPB, 1) fit64_kernel(
     // (4Pi prepares per channel inside the pass.)
     if (MODE != kFit4Pi) w.prepare(cx, st.nt);
     w.template pass<false>(cx, MODE == 7);
+    if (MODE != kFit4Pi && a.handoff) {
+      // Hand-off: the first LM steps in the reference's double arithmetic and
+      // order, then the LM state for the double-float kernels. The step left
+      // pending is the last one whose evaluation the double-float kernel makes.
+      double te[8];
+      if (lane == 0)
+        for (int i = 0; i < 8; i++) te[i] = st.nt[i];
+      int kk = 0, state = Handoff::kCurrent;
+      const int K = a.handoff_iters < a.iterations ? a.handoff_iters : a.iterations;
+      while (kk < K) {
+        if (lane == 0) st.action = lm_control<MODE>(st, a.m, a.s);
+        __syncwarp();
+        const int act = st.action;
+        __syncwarp();
+        if (act == kStop) {
+          state = Handoff::kConverged;
+          break;
+        }
+        ++kk;
+        state = Handoff::kCurrent;
+        if (act == kEval) {
+          if (kk == K) {
+            state = Handoff::kEvalPending;
+            break;
+          }
+          w.prepare(cx, st.nt);
+          w.template pass<false>(cx, false);
+          if (lane == 0)
+            for (int i = 0; i < 8; i++) te[i] = st.nt[i];
+        }
+      }
+      if (lane == 0) {
+        double* r = a.handoff + roi * (int64_t)kHandoffStride;
+        for (int i = 0; i < 8; i++) {
+          const bool in = i < NV;
+          r[Handoff::nt + i] = in ? st.nt[i] : 0.0;
+          r[Handoff::ot + i] = in ? st.ot[i] : 0.0;
+          r[Handoff::ns + i] = in ? st.ns[i] : 0.0;
+          r[Handoff::os + i] = in ? st.os[i] : 0.0;
+          r[Handoff::nc + i] = in ? st.nc[i] : 0.0;
+          r[Handoff::oc + i] = in ? st.oc[i] : 0.0;
+          r[Handoff::te + i] = in ? te[i] : 0.0;
+          r[Handoff::jac + i] = in ? st.jac[i] : 0.0;
+        }
+        for (int i = 0; i < NV * NV; i++) r[Handoff::hes + i] = st.hes[i];
+        r[Handoff::new_lambda] = st.newLambda;
+        r[Handoff::old_lambda] = st.oldLambda;
+        r[Handoff::new_err] = st.newErr;
+        r[Handoff::old_err] = st.oldErr;
+        r[Handoff::sum_update] = st.sumUpdate;
+        r[Handoff::turn] = (double)st.turn;
+        r[Handoff::kk] = (double)kk;
+        r[Handoff::state] = (double)state;
+      }
+      __syncwarp();
+      continue;
+    }
     int kk = 0;
     for (; kk < a.iterations; kk++) {
       if (lane == 0) st.action = lm_control<MODE>(st, a.m, a.s);

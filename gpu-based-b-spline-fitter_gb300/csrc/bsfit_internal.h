@@ -61,12 +61,32 @@ struct FitArgs {
   // launch ends within one ROI's time of its average warp; null: each warp
   // takes every (grid warps)-th ROI. Set by launch_fit.
   unsigned long long* claim;
+  // Double-float kernels only: per-ROI LM state after the first LM steps of
+  // the FP64 reference-order kernel (kHandoffStride doubles per ROI, see
+  // Handoff), or null to start from the initial guess.
+  const double* handoff;
 };
+
+// LM state handed from the FP64 reference-order kernel to the double-float
+// kernels after the first LM steps: per ROI, kHandoffStride doubles at these
+// offsets (parameter arrays of 8).
+struct Handoff {
+  static constexpr int nt = 0, ot = 8, ns = 16, os = 24, nc = 32, oc = 40, te = 48;
+  static constexpr int new_lambda = 56, old_lambda = 57, new_err = 58, old_err = 59,
+                       sum_update = 60, turn = 61, kk = 62, state = 63;
+  static constexpr int jac = 64, hes = 72;  // gradient (8), damped Hessian (8 x 8, row-major NV)
+  // state: 0 an evaluation at nt is pending (the last step was accepted);
+  // 1 the gradient and Hessian of the last evaluation (at te) are current;
+  // 2 converged: the CRLB pass follows.
+  enum { kEvalPending = 0, kCurrent = 1, kConverged = 2 };
+};
+constexpr int kHandoffStride = 136;
 
 constexpr int kMaxStarts = 8;
 
 constexpr int TRACE_REC = 32;
 constexpr int FLAG_NO_REFINE = 1;  // skip the refinement step of the LM solve
+constexpr int FLAG_PARITY = 2;     // double-float parity kernels (bsfit_fitdd.cu)
 
 // Batched form: ROI segments of one fit type fitted by one persistent launch.
 constexpr int kMaxBatchSegs = 48;
@@ -122,6 +142,11 @@ struct Fit64Args {
   const float* dT;
   const float* z0;
   const float* w0;
+  // Hand-off mode (fit types 6, 7, 8): run the initial evaluation and at most
+  // handoff_iters LM steps per ROI, then write the LM state to handoff
+  // (kHandoffStride doubles per ROI) instead of outputs.
+  double* handoff;
+  int handoff_iters;
 };
 
 cudaError_t launch_fit64(const Fit64Args& a, cudaStream_t stream);
@@ -133,6 +158,36 @@ int fit64_smem_bytes(int mode);
 int warp_smem_floats(int mode, int s, bool var = false);
 cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t stream);
 cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream);
+// Double-float parity-grade fit of fit types 6, 7, 8 (plain ROIs, one start).
+cudaError_t launch_fitdd(const FitArgs& a, cudaStream_t stream);
+int fitdd_smem_floats(int mode, int s);
+// One double-float evaluation per ROI (double outputs, layout of launch_eval).
+cudaError_t launch_evaldd(const FitArgs& a, const float* theta, double* out, int fisher,
+                          cudaStream_t stream);
+// Launch shape of a fitter kernel (warps per block among 4, 2, 1 keeping the
+// most warps resident; blocks per SM; SM count), cached per kernel, size and
+// device.
+cudaError_t pick_launch(const void* kern, int per_warp, int* wpb, int* bps, int* sms);
+// The same with the warps per block forced (force_wpb 1, 2 or 4; 0 chooses).
+cudaError_t pick_launch_wpb(const void* kern, int per_warp, int force_wpb, int* wpb, int* bps,
+                            int* sms);
+
+// Autotuner (bsfit_tune.cu): the launch configuration of the single-start FP32
+// fit kernels (plain and batched) per fit type, ROI size and device. variant 0
+// is the default kernel; wpb 0 lets the occupancy choice stand.
+struct TuneConfig {
+  int variant;
+  int wpb;
+};
+using FitKern = void (*)(FitArgs);
+using BatchKern = void (*)(const BatchArgs);
+int tune_num_variants(int mode);
+int tune_min_blocks(int mode, int variant);
+FitKern fit_variant(int mode, int variant);     // variant >= 1
+BatchKern batch_variant(int mode, int variant);  // variant >= 1
+bool tune_lookup(int mode, int s, int dev, TuneConfig* out);
+bool tune_store(int mode, int s, int dev, TuneConfig c);
+void tune_clear(int mode, int s, int dev);
 cudaError_t measure_fp32_peak(double* tflops);
 cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fisher,
                         cudaStream_t stream);

@@ -1,0 +1,102 @@
+// Launch configurations of the FP32 fit kernels chosen by the autotuner.
+//
+// The reference launches every fit with one fixed shape (64-thread blocks, one
+// thread per ROI: VC/GPUmleFit_LM/mexFunction.cpp:407, BlockSize = BSZ). Here
+// the shape of a fit launch has two free parameters whose best values depend on
+// the fit type, the ROI size and the device:
+//  - the kernel variant: the minimum number of resident 4-warp blocks per SM
+//    the kernel is compiled for (__launch_bounds__), which sets its register
+//    budget and so trades registers (and spills) against resident warps;
+//  - the warps per block (4, 2 or 1), which sets how finely the per-warp
+//    shared memory (ROI pixels and maps, growing with the ROI size) packs into
+//    the SM's shared memory.
+// Variant 0 is the default kernel (bsfit_fit.cu); this file instantiates the
+// others. Every variant runs the same code, so results are bit-identical
+// across configurations. A table per (fit type, ROI size, device) holds the
+// chosen configuration; launch_fit and launch_batch consult it.
+#include <mutex>
+
+#include "bsfit_fit_kernels.cuh"
+
+namespace bsfit {
+
+namespace {
+
+constexpr int kMinBlocks6[3] = {BSFIT_MINBLOCKS(6), 5, 4};
+constexpr int kMinBlocks7[3] = {BSFIT_MINBLOCKS(7), 3, 5};
+constexpr int kMinBlocks8[2] = {BSFIT_MINBLOCKS(8), 2};
+
+struct Entry {
+  int mode, s, dev;
+  TuneConfig c;
+};
+std::mutex g_tune_mu;
+constexpr int kMaxEntries = 512;
+Entry g_tune[kMaxEntries];
+int g_ntune = 0;
+
+}  // namespace
+
+int tune_num_variants(int mode) { return mode == 6 ? 3 : mode == 7 ? 3 : mode == 8 ? 2 : 0; }
+
+int tune_min_blocks(int mode, int variant) {
+  if (variant < 0 || variant >= tune_num_variants(mode)) return 0;
+  return mode == 6 ? kMinBlocks6[variant] : mode == 7 ? kMinBlocks7[variant] : kMinBlocks8[variant];
+}
+
+FitKern fit_variant(int mode, int variant) {
+  switch (mode * 10 + variant) {
+    case 61: return fit_kernel<6, false, false, kMinBlocks6[1]>;
+    case 62: return fit_kernel<6, false, false, kMinBlocks6[2]>;
+    case 71: return fit_kernel<7, false, false, kMinBlocks7[1]>;
+    case 72: return fit_kernel<7, false, false, kMinBlocks7[2]>;
+    case 81: return fit_kernel<8, false, false, kMinBlocks8[1]>;
+    default: return nullptr;
+  }
+}
+
+BatchKern batch_variant(int mode, int variant) {
+  switch (mode * 10 + variant) {
+    case 61: return batch_kernel<6, false, kMinBlocks6[1]>;
+    case 62: return batch_kernel<6, false, kMinBlocks6[2]>;
+    case 71: return batch_kernel<7, false, kMinBlocks7[1]>;
+    case 72: return batch_kernel<7, false, kMinBlocks7[2]>;
+    case 81: return batch_kernel<8, false, kMinBlocks8[1]>;
+    default: return nullptr;
+  }
+}
+
+bool tune_lookup(int mode, int s, int dev, TuneConfig* out) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (int i = 0; i < g_ntune; ++i)
+    if (g_tune[i].mode == mode && g_tune[i].s == s && g_tune[i].dev == dev) {
+      *out = g_tune[i].c;
+      return true;
+    }
+  return false;
+}
+
+bool tune_store(int mode, int s, int dev, TuneConfig c) {
+  if (c.variant < 0 || c.variant >= tune_num_variants(mode)) return false;
+  if (c.wpb != 0 && c.wpb != 1 && c.wpb != 2 && c.wpb != 4) return false;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (int i = 0; i < g_ntune; ++i)
+    if (g_tune[i].mode == mode && g_tune[i].s == s && g_tune[i].dev == dev) {
+      g_tune[i].c = c;
+      return true;
+    }
+  if (g_ntune >= kMaxEntries) return false;
+  g_tune[g_ntune++] = Entry{mode, s, dev, c};
+  return true;
+}
+
+void tune_clear(int mode, int s, int dev) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (int i = 0; i < g_ntune; ++i)
+    if (g_tune[i].mode == mode && g_tune[i].s == s && g_tune[i].dev == dev) {
+      g_tune[i] = g_tune[--g_ntune];
+      return;
+    }
+}
+
+}  // namespace bsfit

@@ -136,6 +136,50 @@ int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, i
                      int32_t iterations, float* d_P, float* d_CRLB, float* d_LL, void* stream);
 
 /*
+ * Parity-grade fit (fit types 6, 7, 8): the same method, call and output
+ * layout as bsfit_fit_device, evaluated in double-float arithmetic (two
+ * floats per value, about 48 significant bits) on the FP32 pipe, with the
+ * Fisher matrix inverted in FP64. It follows the trajectory of the
+ * reference's FP64 build (VC/CPUmleFit_LM/CPUmleFit_LM.cpp:2411-3620 with
+ * float promoted to double) as closely as a second FP64 build of the
+ * reference does (one compiled with FMA contraction): the LM's discrete
+ * decisions react to rounding, and the FP32 kernels agree with the FP64
+ * results within the stated tolerances on fewer ROIs (a third of 4D ROIs).
+ * Plain EMCCD ROIs, one start; several times slower than bsfit_fit_device.
+ * Fit type 7's first LM step is taken by the FP64 reference-order kernel of
+ * bsfit_fit_f64_device (its initial Hessian is exactly singular: the
+ * reference's initial pass copies dudt[4] into dudt[5],
+ * CPUmleFit_LM.cpp:2893, so that step is set by the rounding of the
+ * reference's double sums); the model's double tables are made on first use
+ * as for bsfit_fit_f64_device, and the LM state passes through a buffer of
+ * 1088 bytes per ROI from the stream-ordered pool (cudaMallocAsync /
+ * cudaFreeAsync on `stream`). Same work counter as bsfit_fit_device.
+ */
+int bsfit_fit_parity_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                            int64_t nfits, int32_t iterations, float* d_P, float* d_CRLB,
+                            float* d_LL, void* stream);
+
+/* bsfit_fit_parity_device with an explicit number of leading LM steps taken
+ * by the FP64 reference-order kernel (0: none; -1: the default per fit type,
+ * 1 for fit type 7, 0 otherwise). More steps follow the FP64 trajectory
+ * further at the FP64 kernel's speed. */
+int bsfit_fit_parity_steps_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                                  int64_t nfits, int32_t iterations, int32_t exact_steps,
+                                  float* d_P, float* d_CRLB, float* d_LL, void* stream);
+
+/* Host drop-in call of the parity-grade fit: the arguments, checks and
+ * outputs of bsfit_GPUmleFit_LM_multiD (VC/GPUmleFit_LM/mexFunction.cpp:208-762),
+ * fitted by the kernels of bsfit_fit_parity_device. */
+int bsfit_GPUmleFit_LM_multiD_parity(const float* imstack, int64_t roi_size, int64_t roi_size2,
+                                     int64_t nfits, int32_t fittype, int32_t iterations,
+                                     const float* coeff, int32_t coeff_ndim,
+                                     const int64_t* coeff_dims, const float* varmap,
+                                     int64_t varmap_numel, int32_t silent, const float* init_p,
+                                     int64_t init_p_numel, const float* coeff3,
+                                     int32_t coeff3_ndim, const int64_t* coeff3_dims, float* P,
+                                     float* CRLB, float* LL);
+
+/*
  * One model evaluation per ROI at given parameters, without the LM loop: the
  * Poisson deviance, its gradient and the Hessian approximation the reference
  * accumulates (VC/CPUmleFit_LM/CPUmleFit_LM.cpp:2537-2560), or with fisher != 0
@@ -145,6 +189,16 @@ int bsfit_fit_device(bsfit_model model, const float* d_rois, int64_t roi_size, i
  */
 int bsfit_eval_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
                       const float* d_theta, int32_t fisher, float* d_out, void* stream);
+
+/*
+ * bsfit_eval_device in double-float (the evaluation of bsfit_fit_parity_device),
+ * with double outputs in the same per-ROI layout: the deviance (or
+ * log-likelihood), gradient and packed Hessian (or Fisher information) of
+ * VC/CPUmleFit_LM/CPUmleFit_LM.cpp:2537-2560 / :2725-2742 at d_theta.
+ */
+int bsfit_eval_parity_device(bsfit_model model, const float* d_rois, int64_t roi_size,
+                             int64_t nfits, const float* d_theta, int32_t fisher, double* d_out,
+                             void* stream);
 
 /*
  * Diagnostic form of bsfit_fit_device (no counterpart in the reference): also
@@ -278,6 +332,36 @@ int bsfit_server_reset_stats(bsfit_server server);
  */
 #define BSFIT_STATIC_MAX_SEGMENTS 48
 int bsfit_batch_fit_device_static(const bsfit_segment* segs, int32_t nseg, void* stream);
+
+/*
+ * Autotuner (no counterpart in the reference, which launches every fit with
+ * fixed 64-thread blocks, one thread per ROI: VC/GPUmleFit_LM/mexFunction.cpp:407).
+ * The FP32 fit kernels of fit types 6, 7, 8 (single start, EMCCD; plain and
+ * batched) have a launch configuration per fit type, ROI size and device: the
+ * kernel variant (its minimum resident 4-warp blocks per SM, which sets the
+ * register budget: bsfit_tune_min_blocks) and the warps per block (4, 2 or 1;
+ * 0 keeps the occupancy choice). Variant 0 with 0 warps per block is the
+ * default. Every configuration gives bit-identical results. The batched form
+ * uses the configuration of its largest ROI size.
+ */
+int bsfit_tune_num_variants(int32_t fittype);                  /* 0 if none */
+int bsfit_tune_min_blocks(int32_t fittype, int32_t variant);   /* 0 if out of range */
+/* Sets the configuration for (fittype, roi_size) on the current device;
+ * variant -1 restores the default. */
+int bsfit_tune_set(int32_t fittype, int64_t roi_size, int32_t variant, int32_t warps_per_block);
+/* The configuration in force: variant -1 when the default applies. */
+int bsfit_tune_get(int32_t fittype, int64_t roi_size, int32_t* variant, int32_t* warps_per_block);
+/* Times every configuration on the caller's ROIs (a sample of the workload:
+ * one untimed and `reps` timed bsfit_fit_device calls each, CUDA events on
+ * `stream`), sets the fastest for (fit type, roi_size) on the current device
+ * and returns it. all_ms (optional, 3 * bsfit_tune_num_variants doubles):
+ * mean ms per call of (variant v, warps per block 4 / 2 / 1) at
+ * [v * 3 + {0, 1, 2}], -1 where the configuration cannot launch. The outputs
+ * hold the last timed call's results. Synchronises the stream. */
+int bsfit_autotune_device(bsfit_model model, const float* d_rois, int64_t roi_size, int64_t nfits,
+                          int32_t iterations, float* d_P, float* d_CRLB, float* d_LL, int32_t reps,
+                          int32_t* best_variant, int32_t* best_wpb, double* best_ms,
+                          double* all_ms, void* stream);
 
 /*
  * 4Pi fit: four interference channels of one emitter fitted with shared

@@ -63,9 +63,15 @@ class _Base:
 
 
 class Oracle(_Base):
-    """The CPU restatement (``liboracle.so``), FP32 or FP64."""
+    """The CPU restatement (``liboracle.so``), FP32 or FP64. ``fma=True`` loads
+    the build with FMA contraction (``liboracle_fma.so``; raises where the CPU
+    has no FMA)."""
 
-    def __init__(self, path=None):
+    def __init__(self, path=None, fma=False):
+        if path is None and fma:
+            path = _build.build_oracle_fma()
+            if path is None:
+                raise RuntimeError("no FMA on this CPU: the contracted oracle is not built")
         path = path or _build.build_oracle()
         self._lib = ctypes.CDLL(path)
         for fn in ("oracle_fit6_f32", "oracle_fit6_f64", "oracle_fit7_f32", "oracle_fit7_f64",

@@ -21,27 +21,10 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_cases
+from conftest import GOLDEN, Z_NM_PER_UNIT, golden_cases, tol_pass
 
 pytestmark = pytest.mark.gpu
 
-Z_NM_PER_UNIT = 20.0
-
-
-def tol_pass(P, C, R, RC, nv, z_nm=Z_NM_PER_UNIT):
-    ok = np.abs(P[:, :2] - R[:, :2]).max(1) <= 1e-4
-    ok &= np.abs(P[:, 4] - R[:, 4]) * z_nm <= 1e-2
-    with np.errstate(divide="ignore", invalid="ignore"):
-        ok &= np.abs(P[:, 2] / R[:, 2] - 1) <= 1e-5
-        ok &= np.abs(P[:, 3] / R[:, 3] - 1) <= 1e-5
-        for k in range(5, nv):
-            ok &= np.abs(P[:, k] - R[:, k]) <= 1e-4
-        big_r = (RC > 1e25) | ~np.isfinite(RC)
-        big_c = (C > 1e25) | ~np.isfinite(C)
-        relc = np.abs(C / RC - 1)
-        relc[big_r & big_c] = 0
-        ok &= (relc <= 1e-4).all(1)
-    return ok
 
 
 @pytest.fixture(scope="module")
@@ -124,15 +107,21 @@ def test_special_rois_no_crash(bsfit_mod):
     assert np.array_equal(np.isnan(P[:, :5]), np.isnan(R[:, :5]))
 
 
-@pytest.mark.parametrize("fittype,n,min_frac", [(6, 20000, 0.955), (7, 3000, 0.33), (8, 320, 0.0)])
-def test_parity_at_scale(bsfit_mod, oracle, fittype, n, min_frac):
+# Tolerance census of the FP32 kernels at every ROI size of the workloads (3D
+# 11 / 13 / 17 px of the batched headline mix, 4D 13 / 15 px, 5D 17 px): the
+# absolute fraction within the tolerances, and at least the fraction of the
+# reference's own FP32 build on the same ROIs.
+@pytest.mark.parametrize("fittype,s,n,min_frac,stream", [
+    (6, 13, 20000, 0.955, 501), (6, 11, 5000, 0.94, 511), (6, 17, 5000, 0.94, 517),
+    (7, 13, 3000, 0.33, 502), (7, 15, 3000, 0.30, 515), (8, 17, 2000, 0.30, 503)])
+def test_parity_at_scale(bsfit_mod, oracle, fittype, s, n, min_frac, stream):
     from bsfit import workloads as W
     if fittype == 6:
-        wl = W.workload_3d(n, s=13, stream=501)
+        wl = W.workload_3d(n, s=s, stream=stream)
     elif fittype == 7:
-        wl = W.workload_4d(n, sizes=(13,), stream=502)[0]
+        wl = W.workload_4d(n, sizes=(s,), stream=stream)[0]
     else:
-        wl = W.workload_5d(n, stream=503)
+        wl = W.workload_5d(n, s=s, stream=stream)
     nv = {6: 5, 7: 6, 8: 8}[fittype]
     kw = {"initP": wl.init_p} if wl.init_p is not None else {}
     if wl.coeff3 is not None:

@@ -7,7 +7,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import PKG, ROOT
 
 
 def _declared_symbols():
@@ -150,3 +150,24 @@ def test_cpu_call_name_is_the_drop_in():
     a = inspect.signature(bsfit.CPUmleFit_LM).parameters
     b = inspect.signature(bsfit.GPUmleFit_LM_multiD).parameters
     assert list(a) == list(b)
+
+
+def test_double_float_log_table():
+    """The double-float kernels' logarithm table (bsfit_fitdd.cu, kLogTab):
+    entry j holds log(1 + j/128) as the nearest float and the nearest float to
+    the remainder, so hi + lo is within 2^-48 of the value. Recomputed here
+    with 50-digit decimal arithmetic."""
+    import re
+    from decimal import Decimal, getcontext
+    getcontext().prec = 50
+    src = open(os.path.join(PKG, "csrc", "bsfit_fitdd.cu")).read()
+    body = src[src.index("kLogTab[129] = {"):]
+    body = body[:body.index("};")]
+    pairs = re.findall(r"\{([-+0-9.e]+)f, ([-+0-9.e]+)f\}", body)
+    assert len(pairs) == 129
+    for j, (hi, lo) in enumerate(pairs):
+        exact = (Decimal(1) + Decimal(j) / Decimal(128)).ln()
+        h, l_ = np.float32(hi), np.float32(lo)
+        assert h == np.float32(float(exact)), j
+        assert l_ == np.float32(float(exact - Decimal(float(h)))), j
+        assert abs(Decimal(float(h)) + Decimal(float(l_)) - exact) < Decimal(2) ** -48, j

@@ -379,6 +379,33 @@ def bench_serving(args, dev, seed=11):
     g10 = rng.exponential(len(f10) / (0.7 * len(f10) / s10_s) / len(f10), len(f10))
     g10[0] = 0
     _, l10 = run_stream(srv, f10, g10)
+    # 10k-ROI frames drawn from the mixed stream (3D 60%, 4D 25%, 5D 15%) at
+    # 70% of their saturated rate: per-frame latencies, by model too
+    fm = []
+    for i in range(40):
+        kind = rng.choice(["3d", "4d", "5d"], p=[0.6, 0.25, 0.15])
+        w = pools[kind]
+        o = int(rng.integers(0, len(w.rois) - 10000))
+        fm.append((kind, w, np.ascontiguousarray(w.rois[o:o + 10000])))
+    sm_s, _ = run_stream(srv, fm, [0] * len(fm))
+    gm = rng.exponential(sm_s / (0.7 * len(fm)), len(fm))
+    gm[0] = 0
+    lat = []
+    srv.reset_stats()
+    t0 = time.perf_counter()
+    pending = []
+    for (kind, w, r), gap in zip(fm, gm):
+        if gap > 0:
+            target = time.perf_counter() + gap
+            while time.perf_counter() < target:
+                srv.poll()
+        pending.append((kind, time.perf_counter(), srv.submit([(models[kind], r, w.iterations)])))
+    for kind, ts, rid in pending:
+        srv.wait(rid, timeout=300.0)
+    mixed_stats = srv.stats()
+    lat_map = srv.latencies()
+    lat_by = [lat_map.get(rid) for _, _, rid in pending]
+    lat_by = None if any(x is None for x in lat_by) else lat_by
     srv.close()
     # plain per-call form
     t0 = time.perf_counter()
@@ -398,7 +425,25 @@ def bench_serving(args, dev, seed=11):
             "loaded_fits_per_s": n_rois / load_s,
             "frame10k_3d": {"p50_ms": l10["p50_ms"], "p99_ms": l10["p99_ms"], "load": 0.7,
                             "saturated_p50_ms": s10["p50_ms"]},
+            "frame10k_mixed": mixed_frame_summary(fm, lat_by, mixed_stats, sm_s),
             "max_inflight": 4, "arena_bytes": 4 << 30}
+
+
+def mixed_frame_summary(frames, lat_ms, stats, sat_s):
+    """Latency summary of the mixed 10k-ROI frames: overall p50 / p99, the
+    fraction of frames within 5 ms, and per model (lat_ms: per-request
+    latencies in submission order from the server, when available)."""
+    out = {"frames": len(frames), "load": 0.7, "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
+           "saturated_fits_per_s": 10000 * len(frames) / sat_s}
+    if lat_ms is not None and len(lat_ms) == len(frames):
+        lat = np.asarray(lat_ms, float)
+        out["frac_within_5ms"] = float(np.mean(lat <= 5.0))
+        for kind in ("3d", "4d", "5d"):
+            sel = np.array([f[0] == kind for f in frames])
+            if sel.any():
+                out[kind] = {"frames": int(sel.sum()), "p50_ms": float(np.median(lat[sel])),
+                             "p99_ms": float(np.quantile(lat[sel], 0.99))}
+    return out
 
 
 def synthetic_movie(F=64, H=512, W=512, per_frame=150, seed=31, offset=100.0, conversion=0.5):
@@ -480,6 +525,17 @@ def bench_gpu(args):
     stream = torch.cuda.Stream(dev)
     d_rois = [torch.from_numpy(g.rois).to(dev) for g in groups]
     n_step = sum(len(g.rois) for g in groups)
+
+    # Autotuner: each size group's launch configuration (kernel variant,
+    # warps per block) timed on a sample of the group and put in force; the
+    # batched step runs with the configuration of its largest ROI size.
+    tuned = {}
+    if not args.no_tune:
+        from bsfit import tuning as T
+        for g, r in zip(groups, d_rois):
+            ch = T.autotune(models[id(g.coeff)], r[:args.tune_rois], g.iterations, reps=2)
+            tuned[str(g.roi_size)] = {k: ch[k] for k in ("variant", "warps_per_block",
+                                                        "min_blocks", "ms")}
 
     # Batched form: one persistent launch over all size groups per step (the
     # plain form, one call per size group, is timed beside it below).
@@ -792,6 +848,9 @@ def bench_gpu(args):
                        "5d_workload": f"{args.rois_5d} ROIs 17x17, fit type 8, 60 iterations",
                        "4pi_13px": fits_4pi,
                        "4pi_workload": f"{args.rois_4pi} ROIs of 4 channels 13x13, 100 iterations"},
+        "autotune": {"per_size": tuned,
+                     "sample": f"{args.tune_rois} ROIs of each size group",
+                     "batched_uses": str(max(SIZES))} if tuned else None,
         "config_3_colour": c3_fig,
         "config_4_4pi": c4_fig,
         "parity_precision": parity_fig,
@@ -832,6 +891,8 @@ def main():
     ap.add_argument("--rois-parity", type=int, default=100000,
                     help="3D ROIs of the parity-grade figure (4D: half, 5D: a tenth)")
     ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--tune-rois", type=int, default=100000)
     ap.add_argument("--no-prefilter", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-ref-gpu", action="store_true",

@@ -98,7 +98,9 @@ def CPUmleFit_LM(imstack, fittype, iterations=50, coeff=None, varmap=0, silent=1
 class Model:
     """A PSF model whose coefficient tables stay resident on the device."""
 
-    def __init__(self, fittype, coeff, coeff3=None, init_p=None):
+    def __init__(self, fittype, coeff, coeff3=None, init_p=None, tune_cache=None):
+        """tune_cache: a tuning cache file (bsfit.tuning); its choices for this
+        device are put in force for the fits of every model."""
         lib = _native.lib()
         self.fittype = int(fittype)
         self.nv = NUM_PARAMS[self.fittype]
@@ -114,6 +116,9 @@ class Model:
             np.ctypeslib.ctypes.byref(h))
         check(st, "bsfit_model_create")
         self._h = h
+        if tune_cache is not None:
+            from . import tuning
+            tuning.apply_cache(tune_cache, tuning.device_name())
 
     def fit_device(self, d_rois, roi_size, nfits, iterations, d_P, d_CRLB, d_LL, stream=0,
                    precision="f32", exact_steps=-1):
@@ -554,6 +559,17 @@ class Server:
                                                *[ct.byref(x) for x in i]), "bsfit_server_stats")
         return {"p50_ms": d[0].value, "p99_ms": d[1].value, "fits_per_s": d[2].value,
                 "completed": i[0].value, "in_flight": i[1].value, "queued": i[2].value}
+
+    def latencies(self, max_n=100000):
+        """{request id: latency ms} of the requests completed since the last
+        reset_stats."""
+        ct = np.ctypeslib.ctypes
+        ids = (ct.c_int64 * max_n)()
+        ms = (ct.c_double * max_n)()
+        n = ct.c_int32()
+        check(_native.lib().bsfit_server_latencies(self._h, ids, ms, max_n, ct.byref(n)),
+              "bsfit_server_latencies")
+        return {ids[i]: ms[i] for i in range(n.value)}
 
     def reset_stats(self):
         check(_native.lib().bsfit_server_reset_stats(self._h), "bsfit_server_reset_stats")

@@ -81,6 +81,9 @@ SIGNATURES = {
     "bsfit_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                          ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
     "bsfit_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double]),
+    "bsfit_server_latencies": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                              ctypes.POINTER(ctypes.c_double), ctypes.c_int32,
+                                              ctypes.POINTER(ctypes.c_int32)]),
     "bsfit_server_stats": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_double)] * 3 +
                            [ctypes.POINTER(ctypes.c_int64)] * 3),
     "bsfit_server_reset_stats": (ctypes.c_int, [ctypes.c_void_p]),

@@ -128,6 +128,7 @@ struct bsfit_server_s {
   std::deque<Request*> pending;
   std::map<int64_t, Request*> all;  // every request not yet collected
   std::vector<double> latencies_ms;
+  std::vector<int64_t> latency_ids;  // request id of each latencies_ms entry
   int64_t next_id = 1;
   int64_t rois_done = 0;
   Clock::time_point first_submit;
@@ -227,6 +228,7 @@ void retire(bsfit_server_s* s) {
       s->slot_req[i] = nullptr;
       const Clock::time_point done{Clock::duration(r->done_ns.load())};
       s->latencies_ms.push_back(std::chrono::duration<double, std::milli>(done - r->submitted).count());
+      s->latency_ids.push_back(r->id);
       s->rois_done += r->rois;
       if (done > s->last_done) s->last_done = done;
     }
@@ -394,10 +396,25 @@ int bsfit_server_stats(bsfit_server s, double* p50_ms, double* p99_ms, double* f
   return BSFIT_OK;
 }
 
+int bsfit_server_latencies(bsfit_server s, int64_t* ids, double* ms, int32_t max_n,
+                           int32_t* n) {
+  if (!s || !n || max_n < 0 || (max_n > 0 && (!ids || !ms))) return BSFIT_E_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  retire(s);
+  const size_t k = std::min<size_t>((size_t)max_n, s->latencies_ms.size());
+  for (size_t i = 0; i < k; ++i) {
+    ids[i] = s->latency_ids[i];
+    ms[i] = s->latencies_ms[i];
+  }
+  *n = (int32_t)k;
+  return BSFIT_OK;
+}
+
 int bsfit_server_reset_stats(bsfit_server s) {
   if (!s) return BSFIT_E_INVALID;
   std::lock_guard<std::mutex> lock(s->mu);
   s->latencies_ms.clear();
+  s->latency_ids.clear();
   s->rois_done = 0;
   s->any_submit = false;
   return BSFIT_OK;

@@ -314,6 +314,10 @@ int bsfit_server_wait(bsfit_server server, int64_t request_id, double timeout_s)
 int bsfit_server_stats(bsfit_server server, double* p50_ms, double* p99_ms, double* fits_per_s,
                        int64_t* completed, int64_t* in_flight, int64_t* queued);
 int bsfit_server_reset_stats(bsfit_server server);
+/* Per-request latencies (submission to completion, ms) recorded since the last
+ * reset, in completion order: up to max_n (request id, latency) pairs. */
+int bsfit_server_latencies(bsfit_server server, int64_t* ids, double* ms, int32_t max_n,
+                           int32_t* n);
 
 /*
  * Allocation-free batched fit (no counterpart in the reference). For callers

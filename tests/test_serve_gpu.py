@@ -46,6 +46,10 @@ def test_serving_matches_plain_in_the_mix(bsfit_mod):
     st = srv.stats()
     assert st["completed"] == len(frames) and st["in_flight"] == 0 and st["queued"] == 0
     assert st["p99_ms"] >= st["p50_ms"] > 0 and st["fits_per_s"] > 0
+    # per-request latencies: one per request, the quantiles drawn from them
+    lat = srv.latencies()
+    assert sorted(lat) == sorted(ids) and all(v > 0 for v in lat.values())
+    assert min(lat.values()) <= st["p50_ms"] <= st["p99_ms"] <= max(lat.values())
     for rid, (kind, w) in zip(ids, frames):
         kw = {}
         if w.init_p is not None:

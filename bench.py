@@ -585,7 +585,8 @@ def bench_gpu(args):
         per_launch.append(a.elapsed_time(b) / 3)
     plain_ms = sum(per_launch)
     kernel_ms = ms  # the batched step is one kernel launch
-    peak = bsfit.measure_fp32_peak()
+    peak_scalar, peak_paired = bsfit.measure_fp32_peaks()
+    peak = max(peak_scalar, peak_paired)
     achieved = flops / (kernel_ms * 1e-3) * 1e-12
 
     # End to end through the public call: host buffers (pinned), copies and the
@@ -597,7 +598,7 @@ def bench_gpu(args):
     # application's
     host_out = [(np.empty((6, len(g.rois)), np.float32), np.empty((5, len(g.rois)), np.float32),
                  np.empty(len(g.rois), np.float32)) for g in groups]
-    for _ in range(2):
+    for _ in range(3):
         for g, p, o in zip(groups, pinned, host_out):
             bsfit.GPUmleFit_LM_multiD(p, 6, g.iterations, g.coeff, out=o)
     barrier()
@@ -828,8 +829,11 @@ def bench_gpu(args):
                 "step_ms_min": min(e2e_ms), "step_ms_max": max(e2e_ms)},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": "measured FP32 FMA throughput on this device "
-                                    "(bsfit_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
+                     "peak_source": "measured FP32 FMA throughput on this device, the higher of "
+                                    "scalar FFMA and paired FFMA2 chains (bsfit_measure_fp32_peaks); "
+                                    "MEASURED_PEAKS.json has no FP32 figure",
+                     "peak_scalar_tflops": peak_scalar, "peak_paired_tflops": peak_paired,
+                     "peak_theoretical_tflops": 152 * 128 * 2 * 2.07e9 * 1e-12,
                      "flops_per_step": flops, "kernel_ms_per_step": kernel_ms,
                      "per": "launch (the batched step is one persistent launch over all sizes)",
                      "issue": issue},

@@ -673,6 +673,15 @@ def measure_fp32_peak():
     return v.value
 
 
+def measure_fp32_peaks():
+    """(scalar, paired) measured FP32 FMA throughput of the current device,
+    TFLOP/s: scalar FFMA chains and paired FFMA2 chains."""
+    a, b = np.ctypeslib.ctypes.c_double(), np.ctypeslib.ctypes.c_double()
+    check(_native.lib().bsfit_measure_fp32_peaks(np.ctypeslib.ctypes.byref(a),
+                                                 np.ctypeslib.ctypes.byref(b)), "fp32 peaks")
+    return a.value, b.value
+
+
 def eval_flops(fittype, s, channels=1):
     """Algorithmic FLOPs of one ROI evaluation (separable minimum): contract the
     non-lateral axes over the (s+4)^2 knot window, one 4-tap pass per lateral

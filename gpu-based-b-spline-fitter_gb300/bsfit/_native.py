@@ -18,6 +18,8 @@ SIGNATURES = {
     "bsfit_version": (ctypes.c_char_p, []),
     "bsfit_num_params": (ctypes.c_int, [ctypes.c_int32]),
     "bsfit_measure_fp32_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+    "bsfit_measure_fp32_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_double)]),
     "bsfit_GPUmleFit_LM_multiD": (ctypes.c_int, [
         _fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
         _fp, ctypes.c_int32, _i64p, _fp, ctypes.c_int64, ctypes.c_int32, _fp, ctypes.c_int64,

@@ -211,6 +211,11 @@ int bsfit_measure_fp32_peak(double* tflops) {
   return cuda_status(bsfit::measure_fp32_peak(tflops));
 }
 
+int bsfit_measure_fp32_peaks(double* scalar_tflops, double* paired_tflops) {
+  if (!scalar_tflops || !paired_tflops) return BSFIT_E_INVALID;
+  return cuda_status(bsfit::measure_fp32_peak2(scalar_tflops, paired_tflops));
+}
+
 int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
                        const int64_t* coeff_dims, const float* coeff3, int32_t coeff3_ndim,
                        const int64_t* coeff3_dims, const float* init_p, int64_t init_p_numel,

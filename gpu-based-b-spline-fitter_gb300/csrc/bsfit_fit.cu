@@ -187,6 +187,60 @@ __global__ void fp32_peak_kernel(float* out, int iters, float a, float b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// The same with paired FP32 FMAs (FFMA2): 8 independent float2 chains.
+__global__ void fp32x2_peak_kernel(float* out, int iters, float a, float b) {
+  const float t = threadIdx.x * 1e-3f;
+  float2 x0 = make_float2(t, t + 0.5f), x1 = make_float2(t + 1.f, t + 1.5f);
+  float2 x2 = make_float2(t + 2.f, t + 2.5f), x3 = make_float2(t + 3.f, t + 3.5f);
+  float2 x4 = make_float2(t + 4.f, t + 4.5f), x5 = make_float2(t + 5.f, t + 5.5f);
+  float2 x6 = make_float2(t + 6.f, t + 6.5f), x7 = make_float2(t + 7.f, t + 7.5f);
+  const float2 A = make_float2(a, a), B = make_float2(b, b);
+  for (int i = 0; i < iters; ++i) {
+    x0 = __ffma2_rn(x0, A, B); x1 = __ffma2_rn(x1, A, B); x2 = __ffma2_rn(x2, A, B);
+    x3 = __ffma2_rn(x3, A, B); x4 = __ffma2_rn(x4, A, B); x5 = __ffma2_rn(x5, A, B);
+    x6 = __ffma2_rn(x6, A, B); x7 = __ffma2_rn(x7, A, B);
+  }
+  const float2 sum = make_float2(x0.x + x1.x + x2.x + x3.x + x4.x + x5.x + x6.x + x7.x,
+                                 x0.y + x1.y + x2.y + x3.y + x4.y + x5.y + x6.y + x7.y);
+  out[blockIdx.x * blockDim.x + threadIdx.x] = sum.x + sum.y;
+}
+
+cudaError_t measure_fp32_peak2(double* scalar, double* paired) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 1 << 14;
+  float* out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(float) * blocks * threads);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best[2] = {1e30f, 1e30f};
+  for (int kind = 0; kind < 2; ++kind) {
+    if (kind == 0) fp32_peak_kernel<<<blocks, threads>>>(out, 256, 0.999f, 1e-4f);
+    else fp32x2_peak_kernel<<<blocks, threads>>>(out, 256, 0.999f, 1e-4f);
+    for (int r = 0; r < 5; ++r) {
+      cudaEventRecord(e0);
+      if (kind == 0) fp32_peak_kernel<<<blocks, threads>>>(out, iters, 0.999f, 1e-4f);
+      else fp32x2_peak_kernel<<<blocks, threads>>>(out, iters, 0.999f, 1e-4f);
+      cudaEventRecord(e1);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best[kind] = ms < best[kind] ? ms : best[kind];
+    }
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flop = 2.0 * 8.0 * (double)iters * blocks * threads;  // scalar: 8 chains x 2 FLOP
+  *scalar = flop / (best[0] * 1e-3) * 1e-12;
+  *paired = 2.0 * flop / (best[1] * 1e-3) * 1e-12;                  // 2 FMAs per paired op
+  return e;
+}
+
 cudaError_t measure_fp32_peak(double* tflops) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);

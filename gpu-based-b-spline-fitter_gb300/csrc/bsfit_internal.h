@@ -189,6 +189,8 @@ bool tune_lookup(int mode, int s, int dev, TuneConfig* out);
 bool tune_store(int mode, int s, int dev, TuneConfig c);
 void tune_clear(int mode, int s, int dev);
 cudaError_t measure_fp32_peak(double* tflops);
+// FP32 FMA throughput of scalar and of paired (FFMA2) FMA chains, TFLOP/s.
+cudaError_t measure_fp32_peak2(double* scalar, double* paired);
 cudaError_t launch_eval(const FitArgs& a, const float* theta, float* out, int fisher,
                         cudaStream_t stream);
 

@@ -104,6 +104,9 @@ int bsfit_num_params(int32_t fittype);
  * FMA), the roofline denominator of the fitter kernels. No reference
  * counterpart: a measurement utility. */
 int bsfit_measure_fp32_peak(double* tflops);
+/* The same probe with scalar FMA chains and with paired FP32 FMAs (FFMA2, two
+ * FMAs per instruction), TFLOP/s each. */
+int bsfit_measure_fp32_peaks(double* scalar_tflops, double* paired_tflops);
 
 /*
  * Device-resident model: the coefficient tables of one PSF model uploaded once

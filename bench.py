@@ -144,13 +144,28 @@ def bench_kernel_only(args):
     persistent batched launch per step; --model 5d: fit type 8 on --rois ROIs
     of 17 px; --model 4pi: the 4Pi fit of --rois ROIs of four 13 px channels;
     --model 3d64: the FP64 reference-precision kernel on --rois 3D ROIs of 13 px;
-    --model 4d: fit type 7 on --rois ROIs of 13 px."""
+    --model 4d: fit type 7 on --rois ROIs of 13 px. --precision parity runs the
+    double-float kernels on the 3D (13 px), 4D and 5D cases."""
     import torch
     import bsfit
     from bsfit import workloads as W
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(dev)
     launches = args.warmup + args.steps
+    prec = args.precision
+    if prec == "parity" and args.model in ("3d", "4d", "5d"):
+        w = {"3d": lambda: W.workload_3d(args.rois, s=13, stream=9),
+             "4d": lambda: W.workload_4d(args.rois, sizes=(13,), stream=6)[0],
+             "5d": lambda: W.workload_5d(args.rois, s=17, stream=7)}[args.model]()
+        m = bsfit.Model(w.fittype, w.coeff, coeff3=w.coeff3, init_p=w.init_p)
+        r = torch.from_numpy(w.rois).to(dev)
+        with torch.cuda.stream(stream):
+            for _ in range(launches):
+                m.fit_torch(r, w.iterations, stream=stream, precision="parity")
+        stream.synchronize()
+        print(json.dumps({"profile_case": True, "model": args.model, "precision": "parity",
+                          "rois": len(w.rois), "launches": launches}))
+        return 0
     if args.model == "5d":
         w5 = W.workload_5d(args.rois, s=17, stream=7)
         m5 = bsfit.Model(8, w5.coeff, coeff3=w5.coeff3, init_p=w5.init_p)
@@ -882,6 +897,8 @@ def main():
     ap.add_argument("--model", default="3d", choices=["3d", "4d", "5d", "4pi", "3d64"],
                     help="kernel-only: model")
     ap.add_argument("--sizes", type=int, nargs="+", default=list(SIZES))
+    ap.add_argument("--precision", default="f32", choices=["f32", "parity"],
+                    help="kernel-only: the FP32 or the parity-grade (double-float) kernels")
     ap.add_argument("--rois-5d", type=int, default=50000, help="ROIs of the 5D 17 px figure")
     ap.add_argument("--no-5d", action="store_true")
     ap.add_argument("--rois-4d", type=int, default=50000, help="ROIs of the 4D 13 px figure")

@@ -8,7 +8,9 @@
 
 namespace bsfit {
 
-int warp_smem_floats(int mode, int s, bool var) { return make_layout(mode, s, var).total(); }
+int warp_smem_floats(int mode, int s, bool var, int stg) {
+  return make_layout(mode, s, var, stg).total();
+}
 
 // Launch shape of a fitter kernel for a per-warp shared-memory size: the warps
 // per block among 4, 2, 1 that keep the most warps resident per SM, with the
@@ -88,7 +90,6 @@ cudaError_t pick_launch_wpb(const void* kern, int per_warp, int force_wpb, int* 
 
 cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t stream) {
   if (a.nseg <= 0) return cudaSuccess;
-  const int per_warp = warp_smem_floats(mode, a.s_max) * 4;
   void (*kern)(const BatchArgs) = nullptr;
   if (mode == 6 && !multi) kern = batch_kernel<6>;
   else if (mode == 7) kern = multi ? batch_kernel<7, true> : batch_kernel<7>;
@@ -101,6 +102,7 @@ cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t 
       tc.variant > 0)
     kern = batch_variant(mode, tc.variant);
   if (!kern) return cudaErrorInvalidValue;
+  const int per_warp = warp_smem_floats(mode, a.s_max, false, tune_staged(mode, tc.variant)) * 4;
   int wpb = 4, blocks_per_sm = 0, sms = 0;
   cudaError_t e = pick_launch_wpb((const void*)kern, per_warp, multi ? 0 : tc.wpb, &wpb,
                                   &blocks_per_sm, &sms);
@@ -282,7 +284,6 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
   }
   const int mode = a.m.fittype;
   const bool var = a.var != nullptr;
-  const int per_warp = warp_smem_floats(mode, a.s, var) * 4;
   void (*kern)(FitArgs) = nullptr;
   const bool multi = a.n_starts > 1;
   if (var && multi) return cudaErrorInvalidValue;  // not combined
@@ -302,6 +303,8 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
       tc.variant > 0)
     kern = fit_variant(mode, tc.variant);
   if (!kern) return cudaErrorInvalidValue;
+  const int per_warp =
+      warp_smem_floats(mode, a.s, var, tunable ? tune_staged(mode, tc.variant) : 0) * 4;
   int wpb = 4, blocks_per_sm = 0, sms = 0;
   cudaError_t e = pick_launch_wpb((const void*)kern, per_warp, tunable ? tc.wpb : 0, &wpb,
                                   &blocks_per_sm, &sms);

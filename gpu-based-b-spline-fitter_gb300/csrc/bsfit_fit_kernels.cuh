@@ -80,6 +80,16 @@ static __device__ unsigned long long g_phase_cycles[16];
   } while (0)
 #endif
 
+// Asynchronous 4-byte global -> shared copy (cp.async, cached in L1), its
+// group commit and the waits for all but the most recent group / for all.
+__device__ __forceinline__ void cp_async4(float* dst_smem, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <int MODE>
 struct ModeTraits;
 
@@ -163,6 +173,7 @@ struct ModeTraits<8> {
 struct WarpLayout {
   int s, s2p, wp, na, ng, nch, nvar;  // nvar: sCMOS variance planes (0 or nch)
   bool alias;
+  int stage;  // floats of the 5D gather staging buffers (0: gathers go to registers)
   __host__ __device__ static constexpr int bank_pad(int x, int s) {
     return x + ((s - x) % 32 + 32) % 32;
   }
@@ -182,10 +193,18 @@ struct WarpLayout {
   __host__ __device__ constexpr int maps_size() const {
     return (a_rel() + wp * as() > wp * gs()) ? a_rel() + wp * as() : wp * gs();
   }
-  __host__ __device__ constexpr int total() const { return off_maps() + maps_size(); }
+  __host__ __device__ constexpr int off_stage() const { return off_maps() + maps_size(); }
+  __host__ __device__ constexpr int total() const { return off_stage() + stage; }
 };
 
-__host__ __device__ constexpr WarpLayout make_layout(int mode, int s, bool var = false) {
+// Staged 5D gathers: two buffers of kStageQ coefficients (the 4 x 4 x 4 (u, w,
+// z) block of the 5D table and the 4 z values of the 3D table) for 32 nodes,
+// lane-major (coefficient q of the node of lane l at q * 32 + l).
+constexpr int kStageQ = 68;
+constexpr int kStageFloats = 2 * kStageQ * 32;
+
+__host__ __device__ constexpr WarpLayout make_layout(int mode, int s, bool var = false,
+                                                     int stg = 0) {
   WarpLayout L{};
   L.s = s;
   L.s2p = (s * s + 3) & ~3;
@@ -195,6 +214,7 @@ __host__ __device__ constexpr WarpLayout make_layout(int mode, int s, bool var =
   L.nch = mode == kFit4Pi ? k4PiChannels : 1;
   L.nvar = var ? L.nch : 0;
   L.alias = mode == 6 || mode == 8;
+  L.stage = (stg && mode == 8) ? kStageFloats : 0;
   return L;
 }
 
@@ -280,7 +300,7 @@ __device__ __forceinline__ float wrap_phase(float w, int nw) {
 // One image channel of one ROI evaluation: model and derivatives at th for
 // every pixel of `data`, accumulated into this lane's partial sums (err, and
 // acc = gradient 0 .. NV-1, packed Hessian or Fisher upper triangle NV ..).
-template <int MODE, int KP, bool VAR>
+template <int MODE, int KP, bool VAR, int STG = 0>
 __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout& L, float* ws,
                                              const float* data, int lane, const float* th,
                                              bool dup45, bool FISHER, FPair& err,
@@ -474,6 +494,114 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       for (int lz = 0; lz < 2; ++lz)
 #pragma unroll
         for (int lw = 0; lw < 2; ++lw) RP[lz][lw] = make_float2(R[lz][lw][0], R[lz][lw][1]);
+      if constexpr (STG != 0) {
+      // Staged gathers: the 68 coefficients of the next round of 32 nodes are
+      // copied global -> shared with asynchronous copies (cp.async) while the
+      // current round is contracted from shared memory, so each lane has a
+      // round of gathers in flight instead of a few loads; the arithmetic is
+      // that of the unstaged loop, in the same order.
+      float* stg = ws + L.off_stage();
+      const int rounds = (nodes + 31) / 32;
+      auto issue = [&](int r) {
+        const int t = r * 32 + lane;
+        if (t < nodes) {
+          const int xr = t / wy, yr = t - xr * wy;
+          const int64_t lat = (int64_t)(xb + xr) * m.st[1] + (yb + yr);
+          const float* p = base + lat;
+          float* d = stg + (r & 1) * (kStageQ * 32) + lane;
+#pragma unroll
+          for (int iu = 0; iu < 4; ++iu)
+#pragma unroll
+            for (int iw = 0; iw < 4; ++iw)
+#pragma unroll
+              for (int iz = 0; iz < 4; ++iz)
+                cp_async4(d + (((iw * 4 + iu) * 4) + iz) * 32, p + iu * su_ + iw * sw_ + iz * sz_);
+          const float* p3 = base3 + lat;
+#pragma unroll
+          for (int iz = 0; iz < 4; ++iz) cp_async4(d + (64 + iz) * 32, p3 + iz * sz_);
+        }
+        cp_async_commit();
+      };
+      issue(0);
+      for (int r = 0; r < rounds; ++r) {
+        __syncwarp();  // this round's buffer was last read two rounds ago
+        if (r + 1 < rounds) issue(r + 1);
+        else cp_async_commit();
+        cp_async_wait_one();  // this lane's copies of round r have landed
+        const int t = r * 32 + lane;
+        if (t >= nodes) continue;
+        const int xr = t / wy, yr = t - xr * wy;
+        const float* sb = stg + (r & 1) * (kStageQ * 32) + lane;
+        auto S = [&](int iu, int iw, int iz) { return sb[(((iw * 4 + iu) * 4) + iz) * 32]; };
+        // z contraction of the 16 (u, w) columns, u = 2k and 2k + 1 side by
+        // side in one packed operation.
+        float2 vz2[2][4], dzz2[2][4];  // [u pair][w]
+        float2 qz2 = make_float2(0.0f, 0.0f);  // z-term-27 correction, u = 2 | u = 3
+        float2 sq2[2][2];  // [u pair][w in {0,1}]: sum over z in {0,1} of Bz * C
+#pragma unroll
+        for (int iw = 0; iw < 4; ++iw)
+#pragma unroll
+          for (int up = 0; up < 2; ++up) {
+            const float2 c0 = make_float2(S(2 * up, iw, 0), S(2 * up + 1, iw, 0));
+            const float2 c1 = make_float2(S(2 * up, iw, 1), S(2 * up + 1, iw, 1));
+            const float2 c2 = make_float2(S(2 * up, iw, 2), S(2 * up + 1, iw, 2));
+            const float2 c3 = make_float2(S(2 * up, iw, 3), S(2 * up + 1, iw, 3));
+            vz2[up][iw] = contract4x2(c0, c1, c2, c3, BZ0, BZ1, BZ2, BZ3);
+            dzz2[up][iw] = dcontract4x2(c0, c1, c2, c3, DZ0, DZ1, DZ2);
+            if (up == 1 && iw >= 2) {
+              // lvW = iw - 1, lvU = u - 1; Z nodes 1 - lvZ: local 1 (lvZ 1), 0 (lvZ 2)
+              qz2 = __fadd2_rn(qz2, __ffma2_rn(sub2(c2, c1), RP[0][iw - 2],
+                                               __fmul2_rn(sub2(c1, c0), RP[1][iw - 2])));
+            }
+            if (iw <= 1) sq2[up][iw] = __ffma2_rn(c1, BZ1, __fmul2_rn(c0, BZ0));
+          }
+        float vw[4], dzw[4], dww[4];
+#pragma unroll
+        for (int up = 0; up < 2; ++up) {
+          const float2 a = contract4x2(vz2[up][0], vz2[up][1], vz2[up][2], vz2[up][3], BW0, BW1, BW2, BW3);
+          const float2 b = contract4x2(dzz2[up][0], dzz2[up][1], dzz2[up][2], dzz2[up][3], BW0, BW1, BW2, BW3);
+          const float2 c = dcontract4x2(vz2[up][0], vz2[up][1], vz2[up][2], vz2[up][3], DW0, DW1, DW2);
+          vw[2 * up] = a.x;
+          vw[2 * up + 1] = a.y;
+          dzw[2 * up] = b.x;
+          dzw[2 * up + 1] = b.y;
+          dww[2 * up] = c.x;
+          dww[2 * up + 1] = c.y;
+        }
+        const float v = contract4(vw[0], vw[1], vw[2], vw[3], bu[0], bu[1], bu[2], bu[3]);
+        const float dzv = contract4(dzw[0], dzw[1], dzw[2], dzw[3], bu[0], bu[1], bu[2], bu[3]);
+        const float dwv = contract4(dww[0], dww[1], dww[2], dww[3], bu[0], bu[1], bu[2], bu[3]);
+        const float duv = dcontract4(vw[0], vw[1], vw[2], vw[3], du[0], du[1], du[2]);
+        const float qz = qz2.x + qz2.y;
+        float sq[4][2];
+#pragma unroll
+        for (int iw = 0; iw < 2; ++iw) {
+          sq[0][iw] = sq2[0][iw].x;
+          sq[1][iw] = sq2[0][iw].y;
+          sq[2][iw] = sq2[1][iw].x;
+          sq[3][iw] = sq2[1][iw].y;
+        }
+        // u-term-16 correction (CPUsplineLib.cpp:420-421): the term differences
+        // the U node at offset 0 instead of +1 with weight
+        // By1 Bx1 Bz1 Bw1 dBu2(1); lateral side 1 and z, w at offsets -1 / 0.
+        float qu = 0.0f;
+#pragma unroll
+        for (int iw = 0; iw < 2; ++iw)
+          qu += bw[iw] * ((sq[2][iw] - sq[1][iw]) - (sq[3][iw] - sq[2][iw]));
+        qu *= du[2];
+        float e0 = sb[64 * 32], e1 = sb[65 * 32], e2 = sb[66 * 32], e3 = sb[67 * 32];
+        float* o = A + xr * AS + yr;
+        o[0] = v;
+        o[wp] = dzv;
+        o[2 * wp] = dwv;
+        o[3 * wp] = duv;
+        o[4 * wp] = qz;
+        o[5 * wp] = qu;
+        o[6 * wp] = contract4(e0, e1, e2, e3, bz0, bz1, bz2, bz3);
+        o[7 * wp] = dcontract4(e0, e1, e2, e3, dz0, dz1, dz2);
+      }
+      cp_async_wait_all();
+      } else {
       Stride2D ix(lane, wy);
       for (int t = lane; t < nodes; t += 32, ix.next()) {
         const int xr = ix.r, yr = ix.c;
@@ -548,6 +676,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         o[5 * wp] = qu;
         o[6 * wp] = contract4(e0, e1, e2, e3, bz0, bz1, bz2, bz3);
         o[7 * wp] = dcontract4(e0, e1, e2, e3, dz0, dz1, dz2);
+      }
       }
     }
   }
@@ -728,7 +857,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
 
 // Outputs are distributed over the lanes: lane l < NV receives gradient entry
 // l (gl) and Hessian row l (hr), or Fisher row l; err_out is on every lane.
-template <int MODE, bool VAR = false>
+template <int MODE, bool VAR = false, int STG = 0>
 __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int lane,
                          const float* th, bool dup45, bool FISHER, FPair& err_out, float& gl,
                          float (&hr)[ModeTraits<MODE>::NV]) {
@@ -742,7 +871,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
 #pragma unroll
   for (int k = 0; k < KP; ++k) acc[k] = 0.0f;
   if constexpr (TR::NCH == 1) {
-    channel_pass<MODE, KP, VAR>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc);
+    channel_pass<MODE, KP, VAR, STG>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc);
   } else {
     // 4Pi: channel c sees the shared parameters plus its offsets dT[c], with
     // its phase shifted by shift[c] and wrapped; the sums run over all
@@ -984,7 +1113,7 @@ struct RoiResult {
 
 // Fit of the ROI staged in ws (load_roi) from start `start` (0 unless
 // multi-start).
-template <int MODE, bool VAR = false>
+template <int MODE, bool VAR = false, int STG = 0>
 __device__ RoiResult fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, int lane, int64_t roi,
                              int start) {
   using TR = ModeTraits<MODE>;
@@ -1065,7 +1194,7 @@ __device__ RoiResult fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, i
 #pragma unroll
       for (int k = 0; k < NV; ++k)
         the[k] = bcast((MODE == 8 && fisher && k != 2 && k != 3) ? par_eval : par, k);
-      evaluate<MODE, VAR>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr);
+      evaluate<MODE, VAR, STG>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr);
       first = false;
       need_eval = false;
       if (fisher) {
@@ -1379,7 +1508,7 @@ __device__ __forceinline__ void store_result(const FitArgs& a, int lane, int64_t
 // demo_orientation/store/fitb5n3.m:36-45, demo_4pi/bspline_based_4piloc_v4.m:201-214).
 // MULTI selects the multi-start kernels; the single-start ones carry no start
 // loop (it would cost them registers).
-template <int MODE, bool MULTI, bool VAR = false>
+template <int MODE, bool MULTI, bool VAR = false, int STG = 0>
 __device__ __forceinline__ void fit_and_store(const FitArgs& a, const WarpLayout& L, float* ws,
                                               int lane, int64_t roi) {
   load_roi<MODE, VAR>(a, L, ws, lane, roi);
@@ -1395,18 +1524,18 @@ __device__ __forceinline__ void fit_and_store(const FitArgs& a, const WarpLayout
     }
     store_result<MODE>(a, lane, roi, best);
   } else {
-    store_result<MODE>(a, lane, roi, fit_roi<MODE, VAR>(a, L, ws, lane, roi, 0));
+    store_result<MODE>(a, lane, roi, fit_roi<MODE, VAR, STG>(a, L, ws, lane, roi, 0));
   }
 }
 
 // MINB: minimum resident blocks of 4 warps per SM requested from the
 // compiler (its register budget); the default is the measured choice per
 // model, other values are the autotuner's variants (bsfit_tune.cu).
-template <int MODE, bool MULTI, bool VAR = false, int MINB = BSFIT_MINBLOCKS(MODE)>
+template <int MODE, bool MULTI, bool VAR = false, int MINB = BSFIT_MINBLOCKS(MODE), int STG = 0>
 __global__ void __launch_bounds__(128, MINB) fit_kernel(FitArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
-  const WarpLayout L = make_layout(MODE, a.s, VAR);
+  const WarpLayout L = make_layout(MODE, a.s, VAR, STG);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
@@ -1417,13 +1546,13 @@ __global__ void __launch_bounds__(128, MINB) fit_kernel(FitArgs a) {
       if (lane == 0) i = atomicAdd(a.claim, 1ull);
       i = __shfl_sync(kFull, i, 0);
       if ((int64_t)i >= a.nfits) break;
-      fit_and_store<MODE, MULTI, VAR>(a, L, ws, lane, (int64_t)i);
+      fit_and_store<MODE, MULTI, VAR, STG>(a, L, ws, lane, (int64_t)i);
     }
     return;
   }
   const int64_t total_warps = (int64_t)gridDim.x * wpb;
   for (int64_t roi = (int64_t)blockIdx.x * wpb + wib; roi < a.nfits; roi += total_warps)
-    fit_and_store<MODE, MULTI, VAR>(a, L, ws, lane, roi);
+    fit_and_store<MODE, MULTI, VAR, STG>(a, L, ws, lane, roi);
 }
 
 // Persistent batched fit: every warp claims ROIs one at a time from the
@@ -1433,13 +1562,13 @@ __global__ void __launch_bounds__(128, MINB) fit_kernel(FitArgs a) {
 // the largest ROI of the batch. MULTI: every ROI is fitted from its segment's
 // starts and the best log-likelihood kept (fit_and_store), in a separate
 // instantiation so the single-start kernel carries no start loop.
-template <int MODE, bool MULTI = false, int MINB = BSFIT_MINBLOCKS(MODE)>
+template <int MODE, bool MULTI = false, int MINB = BSFIT_MINBLOCKS(MODE), int STG = 0>
 __global__ void __launch_bounds__(128, MINB) batch_kernel(const __grid_constant__ BatchArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* ws = smem + wib * make_layout(MODE, a.s_max).total();
+  float* ws = smem + wib * make_layout(MODE, a.s_max, false, STG).total();
   int seg = 0;
   while (seg < a.nseg) {
     const BatchSeg& g = a.seg[seg];
@@ -1479,7 +1608,7 @@ __global__ void __launch_bounds__(128, MINB) batch_kernel(const __grid_constant_
 #pragma unroll
         for (int j = 0; j < 4; ++j) fa.starts[k][j] = g.starts[k][j];
     }
-    fit_and_store<MODE, MULTI>(fa, make_layout(MODE, g.s), ws, lane, (int64_t)i);
+    fit_and_store<MODE, MULTI, false, STG>(fa, make_layout(MODE, g.s, false, STG), ws, lane, (int64_t)i);
     if (lane == 0) atomicAdd(&a.done[g.slot], 1ull);
   }
 }

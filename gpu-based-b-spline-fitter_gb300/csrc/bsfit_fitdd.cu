@@ -1324,8 +1324,11 @@ __device__ Result fit_roi(const FitArgs& a, const Layout& L, float* ws, int lane
   return Result{to_f(par), crlb, to_f(ll), kk};
 }
 
+// Minimum resident 4-warp blocks per SM: 3D fits in 128 registers (16 warps per
+// SM, 4 bytes of spill); 4D and 5D keep their register need (167 and 255; a
+// 128-register cap spills 0.5 and 1.5 KB per thread).
 template <int MODE>
-__global__ void __launch_bounds__(128) fitdd_kernel(FitArgs a) {
+__global__ void __launch_bounds__(128, MODE == 6 ? 4 : 1) fitdd_kernel(FitArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
   constexpr int NV = Traits<MODE>::NV;

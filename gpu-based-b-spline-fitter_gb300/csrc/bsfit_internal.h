@@ -155,7 +155,7 @@ cudaError_t widen_to_f64(const float* src, double* dst, int64_t total, int naxes
                          const int64_t* strides, cudaStream_t stream);
 int fit64_smem_bytes(int mode);
 
-int warp_smem_floats(int mode, int s, bool var = false);
+int warp_smem_floats(int mode, int s, bool var = false, int stg = 0);
 cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t stream);
 cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream);
 // Double-float parity-grade fit of fit types 6, 7, 8 (plain ROIs, one start).
@@ -183,6 +183,9 @@ using FitKern = void (*)(FitArgs);
 using BatchKern = void (*)(const BatchArgs);
 int tune_num_variants(int mode);
 int tune_min_blocks(int mode, int variant);
+// 1 when the variant stages the 5D gathers through shared memory (its
+// per-warp shared memory includes the staging buffers)
+int tune_staged(int mode, int variant);
 FitKern fit_variant(int mode, int variant);     // variant >= 1
 BatchKern batch_variant(int mode, int variant);  // variant >= 1
 bool tune_lookup(int mode, int s, int dev, TuneConfig* out);

@@ -9,7 +9,9 @@
 //    budget and so trades registers (and spills) against resident warps;
 //  - the warps per block (4, 2 or 1), which sets how finely the per-warp
 //    shared memory (ROI pixels and maps, growing with the ROI size) packs into
-//    the SM's shared memory.
+//    the SM's shared memory;
+//  - for fit type 8, the staging of stage A's gathers: into registers, or into
+//    shared memory with asynchronous copies one round of 32 nodes ahead.
 // Variant 0 is the default kernel (bsfit_fit.cu); this file instantiates the
 // others. Every variant runs the same code, so results are bit-identical
 // across configurations. A table per (fit type, ROI size, device) holds the
@@ -24,7 +26,10 @@ namespace {
 
 constexpr int kMinBlocks6[3] = {BSFIT_MINBLOCKS(6), 5, 4};
 constexpr int kMinBlocks7[3] = {BSFIT_MINBLOCKS(7), 3, 5};
-constexpr int kMinBlocks8[2] = {BSFIT_MINBLOCKS(8), 2};
+// fit type 8: variants 2 and 3 stage the 5D gathers through shared memory
+// (cp.async, two rounds of 32 nodes in flight per warp)
+constexpr int kMinBlocks8[4] = {BSFIT_MINBLOCKS(8), 2, 2, 1};
+constexpr bool kStaged8[4] = {false, false, true, true};
 
 struct Entry {
   int mode, s, dev;
@@ -37,7 +42,11 @@ int g_ntune = 0;
 
 }  // namespace
 
-int tune_num_variants(int mode) { return mode == 6 ? 3 : mode == 7 ? 3 : mode == 8 ? 2 : 0; }
+int tune_num_variants(int mode) { return mode == 6 ? 3 : mode == 7 ? 3 : mode == 8 ? 4 : 0; }
+
+int tune_staged(int mode, int variant) {
+  return (mode == 8 && variant >= 0 && variant < 4 && kStaged8[variant]) ? 1 : 0;
+}
 
 int tune_min_blocks(int mode, int variant) {
   if (variant < 0 || variant >= tune_num_variants(mode)) return 0;
@@ -51,6 +60,8 @@ FitKern fit_variant(int mode, int variant) {
     case 71: return fit_kernel<7, false, false, kMinBlocks7[1]>;
     case 72: return fit_kernel<7, false, false, kMinBlocks7[2]>;
     case 81: return fit_kernel<8, false, false, kMinBlocks8[1]>;
+    case 82: return fit_kernel<8, false, false, kMinBlocks8[2], 1>;
+    case 83: return fit_kernel<8, false, false, kMinBlocks8[3], 1>;
     default: return nullptr;
   }
 }
@@ -62,6 +73,8 @@ BatchKern batch_variant(int mode, int variant) {
     case 71: return batch_kernel<7, false, kMinBlocks7[1]>;
     case 72: return batch_kernel<7, false, kMinBlocks7[2]>;
     case 81: return batch_kernel<8, false, kMinBlocks8[1]>;
+    case 82: return batch_kernel<8, false, kMinBlocks8[2], 1>;
+    case 83: return batch_kernel<8, false, kMinBlocks8[3], 1>;
     default: return nullptr;
   }
 }

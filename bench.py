@@ -402,25 +402,39 @@ def bench_serving(args, dev, seed=11):
         w = pools[kind]
         o = int(rng.integers(0, len(w.rois) - 10000))
         fm.append((kind, w, np.ascontiguousarray(w.rois[o:o + 10000])))
-    sm_s, _ = run_stream(srv, fm, [0] * len(fm))
-    gm = rng.exponential(sm_s / (0.7 * len(fm)), len(fm))
-    gm[0] = 0
-    lat = []
-    srv.reset_stats()
-    t0 = time.perf_counter()
-    pending = []
-    for (kind, w, r), gap in zip(fm, gm):
-        if gap > 0:
-            target = time.perf_counter() + gap
-            while time.perf_counter() < target:
-                srv.poll()
-        pending.append((kind, time.perf_counter(), srv.submit([(models[kind], r, w.iterations)])))
-    for kind, ts, rid in pending:
-        srv.wait(rid, timeout=300.0)
-    mixed_stats = srv.stats()
-    lat_map = srv.latencies()
-    lat_by = [lat_map.get(rid) for _, _, rid in pending]
-    lat_by = None if any(x is None for x in lat_by) else lat_by
+    unit_gaps = rng.exponential(1.0, len(fm))
+    unit_gaps[0] = 0
+
+    def mixed10k(srv, offered_s=None):
+        """Saturated pass, then the frames with Poisson arrivals at 70% of the
+        saturated rate (of offered_s, a saturated time, when given: the same
+        arrivals for two servers)."""
+        sm_s, _ = run_stream(srv, fm, [0] * len(fm))
+        gm = unit_gaps * (offered_s or sm_s) / (0.7 * len(fm))
+        srv.reset_stats()
+        pending = []
+        for (kind, w, r), gap in zip(fm, gm):
+            if gap > 0:
+                target = time.perf_counter() + gap
+                while time.perf_counter() < target:
+                    srv.poll()
+            pending.append((kind, time.perf_counter(), srv.submit([(models[kind], r, w.iterations)])))
+        for kind, ts, rid in pending:
+            srv.wait(rid, timeout=300.0)
+        mixed_stats = srv.stats()
+        lat_map = srv.latencies()
+        lat_by = [lat_map.get(rid) for _, _, rid in pending]
+        lat_by = None if any(x is None for x in lat_by) else lat_by
+        return sm_s, mixed_frame_summary(fm, lat_by, mixed_stats, sm_s)
+
+    fm_sat_s, mixed = mixed10k(srv)
+    srv.close()
+    # merged admission: a free slot takes up to 4 queued requests into one launch
+    srv = bsfit.Server(max_inflight=4, arena_bytes=4 << 30, merge=4)
+    run_stream(srv, frames[:4], [0] * 4)  # warm-up
+    msat_s, _ = run_stream(srv, frames, [0] * len(frames))
+    merged = {"merge": 4, "fits_per_s": n_rois / msat_s,
+              "frame10k_mixed": mixed10k(srv, fm_sat_s)[1]}
     srv.close()
     # plain per-call form
     t0 = time.perf_counter()
@@ -440,7 +454,7 @@ def bench_serving(args, dev, seed=11):
             "loaded_fits_per_s": n_rois / load_s,
             "frame10k_3d": {"p50_ms": l10["p50_ms"], "p99_ms": l10["p99_ms"], "load": 0.7,
                             "saturated_p50_ms": s10["p50_ms"]},
-            "frame10k_mixed": mixed_frame_summary(fm, lat_by, mixed_stats, sm_s),
+            "frame10k_mixed": mixed, "merged": merged,
             "max_inflight": 4, "arena_bytes": 4 << 30}
 
 

@@ -481,11 +481,17 @@ class Server:
     the last call (P (N, NV+1), CRLB (N, NV), LL (N,) per segment, as
     GPUmleFit_LM_multiD); wait(id) blocks until one request is done."""
 
-    def __init__(self, max_inflight=4, arena_bytes=2 << 30):
+    def __init__(self, max_inflight=4, arena_bytes=2 << 30, merge=1):
+        """merge: most queued requests fitted by one launch (bsfit_server_set_merge)."""
         h = np.ctypeslib.ctypes.c_void_p()
         check(_native.lib().bsfit_server_create(int(max_inflight), int(arena_bytes),
                                                 np.ctypeslib.ctypes.byref(h)), "bsfit_server_create")
         self._h = h
+        if merge != 1:
+            st = _native.lib().bsfit_server_set_merge(h, int(merge))
+            if st != 0:
+                self.close()
+                check(st, "bsfit_server_set_merge")
         self._live = {}
         self._done = {}  # results collected by poll() and not yet taken by wait()
 

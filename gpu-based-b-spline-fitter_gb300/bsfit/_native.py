@@ -75,6 +75,7 @@ SIGNATURES = {
     "bsfit_server_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64,
                                            ctypes.POINTER(ctypes.c_void_p)]),
     "bsfit_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "bsfit_server_set_merge": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "bsfit_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                            ctypes.POINTER(ctypes.c_int64)]),
     "bsfit_server_submit_multistart": (ctypes.c_int, [

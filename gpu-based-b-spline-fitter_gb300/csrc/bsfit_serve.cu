@@ -13,6 +13,10 @@
 //    launch and device-to-host copies on its slot's stream, so requests in
 //    flight overlap on the GPU (a new request's blocks start as the running
 //    ones retire);
+//  - optionally (bsfit_server_set_merge), a free slot takes several queued
+//    single-start requests at once and fits all their segments in one
+//    persistent launch, each request still copied back and completed on its
+//    own;
 //  - a host callback at the end of the stream marks the request done with its
 //    completion time, so results are returned per request as soon as they are
 //    ready and the latency (submit to completion) is exact.
@@ -107,8 +111,13 @@ void CUDART_CB on_done(void* p) {
   r->finished.store(1, std::memory_order_release);
 }
 
+// Work-queue counters at the start of a request's arena block: room for a
+// merged launch of up to BSFIT_MAX_SEGMENTS segments, so the first request of a
+// merged group holds the group's counters.
+constexpr int64_t kCounterBytes = 256 + (int64_t)BSFIT_MAX_SEGMENTS * 2 * 8;
+
 int64_t request_bytes(const std::vector<bsfit_host_segment>& segs) {
-  int64_t b = 256 + (int64_t)segs.size() * 2 * 8;  // work-queue counters
+  int64_t b = kCounterBytes;
   for (const auto& g : segs) {
     const int nv = bsfit_num_params(bsfit_model_fittype(g.model));
     b += (g.nfits * g.roi_size * g.roi_size * 4 + 255) / 256 * 256;
@@ -124,7 +133,8 @@ struct bsfit_server_s {
   char* arena_base = nullptr;
   Arena arena;
   std::vector<cudaStream_t> streams;
-  std::vector<Request*> slot_req;  // request running in each slot, or null
+  std::vector<std::vector<Request*>> slot_req;  // requests running in each slot (empty: free)
+  int merge = 1;  // most queued requests fitted by one launch
   std::deque<Request*> pending;
   std::map<int64_t, Request*> all;  // every request not yet collected
   std::vector<double> latencies_ms;
@@ -139,100 +149,135 @@ struct bsfit_server_s {
 
 namespace {
 
-// Enqueue an admitted request on its slot's stream. Caller holds the mutex.
-int launch_request(bsfit_server_s* s, Request* r) {
-  cudaStream_t st = s->streams[r->slot];
-  char* base = s->arena_base + r->offset;
-  int64_t off = 0;
-  unsigned long long* scratch = (unsigned long long*)base;
-  off += 256 + (int64_t)r->segs.size() * 2 * 8;
-  off = (off + 255) / 256 * 256;
-  std::vector<bsfit_segment> dsegs(r->segs.size());
+// Enqueue an admitted group of requests on their slot's stream: every
+// request's uploads, one batched launch over all their segments (the first
+// request's block holds the group's work-queue counters), then every request's
+// result copies and completion callback. Caller holds the mutex.
+int launch_group(bsfit_server_s* s, int slot, const std::vector<Request*>& grp) {
+  cudaStream_t st = s->streams[slot];
+  std::vector<bsfit_segment> dsegs;
+  std::vector<bsfit_starts> starts;
   cudaError_t e = cudaSuccess;
-  for (size_t i = 0; i < r->segs.size(); ++i) {
-    const bsfit_host_segment& g = r->segs[i];
-    const int nv = bsfit_num_params(bsfit_model_fittype(g.model));
-    const int64_t rb = g.nfits * g.roi_size * g.roi_size * 4;
-    float* d_rois = (float*)(base + off);
-    off += (rb + 255) / 256 * 256;
-    float* d_out = (float*)(base + off);
-    off += ((int64_t)g.nfits * (2 * nv + 2) * 4 + 255) / 256 * 256;
-    if (e == cudaSuccess && rb > 0) e = cudaMemcpyAsync(d_rois, g.rois, rb, cudaMemcpyHostToDevice, st);
-    bsfit_segment& d = dsegs[i];
-    d.model = g.model;
-    d.d_rois = d_rois;
-    d.roi_size = g.roi_size;
-    d.nfits = g.nfits;
-    d.iterations = g.iterations;
-    d.d_P = d_out;
-    d.d_CRLB = d_out + g.nfits * (nv + 1);
-    d.d_LL = d.d_CRLB + g.nfits * nv;
+  for (Request* r : grp) {
+    char* base = s->arena_base + r->offset;
+    int64_t off = kCounterBytes;
+    for (size_t i = 0; i < r->segs.size(); ++i) {
+      const bsfit_host_segment& g = r->segs[i];
+      const int nv = bsfit_num_params(bsfit_model_fittype(g.model));
+      const int64_t rb = g.nfits * g.roi_size * g.roi_size * 4;
+      float* d_rois = (float*)(base + off);
+      off += (rb + 255) / 256 * 256;
+      float* d_out = (float*)(base + off);
+      off += ((int64_t)g.nfits * (2 * nv + 2) * 4 + 255) / 256 * 256;
+      if (e == cudaSuccess && rb > 0) e = cudaMemcpyAsync(d_rois, g.rois, rb, cudaMemcpyHostToDevice, st);
+      bsfit_segment d;
+      d.model = g.model;
+      d.d_rois = d_rois;
+      d.roi_size = g.roi_size;
+      d.nfits = g.nfits;
+      d.iterations = g.iterations;
+      d.d_P = d_out;
+      d.d_CRLB = d_out + g.nfits * (nv + 1);
+      d.d_LL = d.d_CRLB + g.nfits * nv;
+      dsegs.push_back(d);
+    }
+    for (const auto& q : r->starts) starts.push_back(q);
   }
   if (e != cudaSuccess) return cuda_status_s(e);
+  void* scratch = s->arena_base + grp[0]->offset;
   const int64_t sb = bsfit_batch_scratch_bytes((int32_t)dsegs.size());
-  int stt = r->starts.empty()
+  int stt = starts.empty()
                 ? bsfit_batch_fit_device(dsegs.data(), (int32_t)dsegs.size(), scratch, sb, st)
-                : bsfit_batch_fit_multistart_device(dsegs.data(), r->starts.data(),
+                : bsfit_batch_fit_multistart_device(dsegs.data(), starts.data(),
                                                     (int32_t)dsegs.size(), scratch, sb, st);
   if (stt != BSFIT_OK) return stt;
-  for (size_t i = 0; i < r->segs.size(); ++i) {
-    const bsfit_host_segment& g = r->segs[i];
-    const int nv = bsfit_num_params(bsfit_model_fittype(g.model));
-    if (g.nfits == 0) continue;
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(g.P, dsegs[i].d_P, (size_t)g.nfits * (nv + 1) * 4, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(g.CRLB, dsegs[i].d_CRLB, (size_t)g.nfits * nv * 4, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(g.LL, dsegs[i].d_LL, (size_t)g.nfits * 4, cudaMemcpyDeviceToHost, st);
+  size_t k = 0;
+  for (Request* r : grp) {
+    for (size_t i = 0; i < r->segs.size(); ++i, ++k) {
+      const bsfit_host_segment& g = r->segs[i];
+      const int nv = bsfit_num_params(bsfit_model_fittype(g.model));
+      if (g.nfits == 0) continue;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g.P, dsegs[k].d_P, (size_t)g.nfits * (nv + 1) * 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g.CRLB, dsegs[k].d_CRLB, (size_t)g.nfits * nv * 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g.LL, dsegs[k].d_LL, (size_t)g.nfits * 4, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaLaunchHostFunc(st, on_done, r);
   }
-  if (e == cudaSuccess) e = cudaLaunchHostFunc(st, on_done, r);
   return cuda_status_s(e);
 }
 
 // Admit pending requests while slots and arena space allow (submission order).
+// A free slot takes the oldest request and, with merging on, the next queued
+// single-start requests that fit the arena, up to `merge` requests and
+// BSFIT_MAX_SEGMENTS segments per launch.
 void admit(bsfit_server_s* s) {
   while (!s->pending.empty()) {
     int slot = -1;
     for (size_t i = 0; i < s->slot_req.size(); ++i)
-      if (!s->slot_req[i]) {
+      if (s->slot_req[i].empty()) {
         slot = (int)i;
         break;
       }
     if (slot < 0) return;
-    Request* r = s->pending.front();
-    int64_t off = s->arena.alloc(r->bytes);
-    if (off < 0) return;  // wait for memory to free up
-    s->pending.pop_front();
-    r->offset = off;
-    r->slot = slot;
-    r->started = Clock::now();
-    s->slot_req[slot] = r;
-    int st = launch_request(s, r);
+    std::vector<Request*> grp;
+    size_t nseg = 0;
+    while (!s->pending.empty() && (int)grp.size() < s->merge) {
+      Request* r = s->pending.front();
+      if (!grp.empty() && (!r->starts.empty() || !grp[0]->starts.empty() ||
+                           nseg + r->segs.size() > (size_t)BSFIT_MAX_SEGMENTS))
+        break;
+      int64_t off = s->arena.alloc(r->bytes);
+      if (off < 0) break;  // wait for memory to free up
+      s->pending.pop_front();
+      r->offset = off;
+      r->slot = slot;
+      r->started = Clock::now();
+      grp.push_back(r);
+      nseg += r->segs.size();
+    }
+    if (grp.empty()) return;
+    s->slot_req[slot] = grp;
+    int st = launch_group(s, slot, grp);
     if (st != BSFIT_OK) {
-      // The request failed to launch: complete it with the error.
-      r->status = st;
+      // The group failed to launch: complete its requests with the error.
       cudaStreamSynchronize(s->streams[slot]);
-      r->done_ns.store(Clock::now().time_since_epoch().count());
-      r->finished.store(1);
+      for (Request* r : grp) {
+        r->status = st;
+        r->done_ns.store(Clock::now().time_since_epoch().count());
+        r->finished.store(1);
+      }
     }
   }
 }
 
-// Retire finished requests: free their slot and arena space.
+// Retire finished groups: free their slot and their requests' arena space.
 void retire(bsfit_server_s* s) {
   for (size_t i = 0; i < s->slot_req.size(); ++i) {
-    Request* r = s->slot_req[i];
-    if (r && r->finished.load(std::memory_order_acquire)) {
+    std::vector<Request*>& grp = s->slot_req[i];
+    if (grp.empty()) continue;
+    bool all = true;
+    for (Request* r : grp) all = all && r->finished.load(std::memory_order_acquire);
+    if (!all) continue;
+    for (Request* r : grp) {
       s->arena.release(r->offset, r->bytes);
-      s->slot_req[i] = nullptr;
       const Clock::time_point done{Clock::duration(r->done_ns.load())};
       s->latencies_ms.push_back(std::chrono::duration<double, std::milli>(done - r->submitted).count());
       s->latency_ids.push_back(r->id);
       s->rois_done += r->rois;
       if (done > s->last_done) s->last_done = done;
     }
+    grp.clear();
   }
+}
+
+bool running(const bsfit_server_s* s, const Request* r) {
+  for (const auto& grp : s->slot_req)
+    for (const Request* q : grp)
+      if (q == r) return true;
+  return false;
 }
 
 }  // namespace
@@ -252,7 +297,7 @@ int bsfit_server_create(int32_t max_inflight, int64_t arena_bytes, bsfit_server*
   }
   s->arena.init(arena_bytes);
   s->streams.resize(max_inflight, nullptr);
-  s->slot_req.assign(max_inflight, nullptr);
+  s->slot_req.assign(max_inflight, {});
   for (int i = 0; i < max_inflight && e == cudaSuccess; ++i)
     e = cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -263,6 +308,14 @@ int bsfit_server_create(int32_t max_inflight, int64_t arena_bytes, bsfit_server*
     return cuda_status_s(e);
   }
   *out = s;
+  return BSFIT_OK;
+}
+
+int bsfit_server_set_merge(bsfit_server s, int32_t max_requests_per_launch) {
+  if (!s || max_requests_per_launch < 1 || max_requests_per_launch > BSFIT_MAX_SEGMENTS)
+    return BSFIT_E_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->merge = max_requests_per_launch;
   return BSFIT_OK;
 }
 
@@ -330,9 +383,7 @@ int bsfit_server_poll(bsfit_server s, int64_t* done_ids, int32_t max_ids, int32_
   int n = 0;
   for (auto it = s->all.begin(); it != s->all.end() && n < max_ids;) {
     Request* r = it->second;
-    bool running = false;
-    for (auto q : s->slot_req) running |= (q == r);
-    if (r->finished.load(std::memory_order_acquire) && !running) {
+    if (r->finished.load(std::memory_order_acquire) && !running(s, r)) {
       done_ids[n++] = r->id;
       delete r;
       it = s->all.erase(it);
@@ -356,9 +407,7 @@ int bsfit_server_wait(bsfit_server s, int64_t request_id, double timeout_s) {
       auto it = s->all.find(request_id);
       if (it == s->all.end()) return BSFIT_E_INVALID;  // unknown or already collected
       Request* r = it->second;
-      bool running = false;
-      for (auto q : s->slot_req) running |= (q == r);
-      if (r->finished.load(std::memory_order_acquire) && !running) {
+      if (r->finished.load(std::memory_order_acquire) && !running(s, r)) {
         int st = r->status;
         delete r;
         s->all.erase(it);
@@ -390,7 +439,7 @@ int bsfit_server_stats(bsfit_server s, double* p50_ms, double* p99_ms, double* f
   }
   if (completed) *completed = (int64_t)s->latencies_ms.size();
   int64_t fl = 0;
-  for (auto r : s->slot_req) fl += (r != nullptr);
+  for (const auto& grp : s->slot_req) fl += (int64_t)grp.size();
   if (in_flight) *in_flight = fl;
   if (queued) *queued = (int64_t)s->pending.size();
   return BSFIT_OK;

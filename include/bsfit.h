@@ -296,6 +296,13 @@ typedef struct bsfit_server_s* bsfit_server;
 
 int bsfit_server_create(int32_t max_inflight, int64_t arena_bytes, bsfit_server* out);
 int bsfit_server_destroy(bsfit_server server);
+/* Requests fitted by one launch: a free slot takes the oldest queued request
+ * and up to max_requests_per_launch - 1 more queued single-start requests
+ * that fit the arena (at most BSFIT_MAX_SEGMENTS segments in all), fitted by one
+ * persistent batched launch; each request is still copied back and completed
+ * on its own. 1 (the default) launches every request alone. Results do not
+ * depend on the setting. */
+int bsfit_server_set_merge(bsfit_server server, int32_t max_requests_per_launch);
 /* As bsfit_server_submit, with per-segment starts (bsfit_starts, see
  * bsfit_batch_fit_multistart_device): the request's fits run the callers'
  * multi-start inside the batched launch. */

@@ -134,3 +134,46 @@ def test_serving_multistart_matches_plain(bsfit_mod):
         assert np.array_equal(Cs, C.T, equal_nan=True)
         assert np.array_equal(Ls, L, equal_nan=True)
     srv.close()
+
+
+def test_serving_merged_launches_match_plain(bsfit_mod):
+    """With merging on (bsfit_server_set_merge), queued single-start requests of
+    mixed models fitted by shared launches give each request the plain call's
+    results bit for bit; a multi-start request among them runs alone and is
+    unchanged; every request is completed and collected once."""
+    frames = _frames() * 2
+    models = {}
+    for kind, w in frames:
+        if kind not in models:
+            models[kind] = bsfit_mod.Model(w.fittype, w.coeff, coeff3=w.coeff3, init_p=w.init_p)
+    srv = bsfit_mod.Server(max_inflight=2, arena_bytes=96 << 20, merge=4)
+    ids = [srv.submit([(models[kind], w.rois, w.iterations)]) for kind, w in frames]
+    w4 = frames[4][1]
+    z, wv = float(w4.init_p[0]), float(w4.init_p[1])
+    st4 = np.array([[1.2 * z, wv], [z, wv]], np.float32)
+    ms = srv.submit([(models["4d"], w4.rois, w4.iterations)], starts=[st4])
+    ids2 = [srv.submit([(models[kind], w.rois, w.iterations)]) for kind, w in frames[:3]]
+    results = {rid: srv.wait(rid, timeout=120.0) for rid in ids + [ms] + ids2}
+    st = srv.stats()
+    assert st["completed"] == len(results) and st["in_flight"] == 0 and st["queued"] == 0
+    assert sorted(srv.latencies()) == sorted(results)
+    for rid, (kind, w) in list(zip(ids, frames)) + list(zip(ids2, frames[:3])):
+        kw = {}
+        if w.init_p is not None:
+            kw["initP"] = w.init_p
+        if w.coeff3 is not None:
+            kw["coeff3"] = w.coeff3
+        P, C, L = bsfit_mod.GPUmleFit_LM_multiD(w.rois, w.fittype, w.iterations, w.coeff, **kw)
+        Ps, Cs, Ls = results[rid][0]
+        assert np.array_equal(Ps, P, equal_nan=True), kind
+        assert np.array_equal(Cs, C, equal_nan=True), kind
+        assert np.array_equal(Ls, L, equal_nan=True), kind
+    import torch
+    P, C, L = (x.cpu().numpy() for x in models["4d"].fit_multistart_torch(
+        torch.from_numpy(w4.rois).cuda(), w4.iterations, st4))
+    Ps, Cs, Ls = results[ms][0]
+    assert np.array_equal(Ps, P.T, equal_nan=True)
+    assert np.array_equal(Ls, L, equal_nan=True)
+    with pytest.raises(bsfit_mod.BsfitError):
+        bsfit_mod.Server(max_inflight=1, arena_bytes=1 << 20, merge=0)
+    srv.close()

@@ -33,6 +33,7 @@ SIGNATURES = {
         ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
     "bsfit_tune_num_variants": (ctypes.c_int, [ctypes.c_int32]),
     "bsfit_tune_min_blocks": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
+    "bsfit_tune_rois_per_warp": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
     "bsfit_tune_set": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
                                       ctypes.c_int32]),
     "bsfit_tune_get": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64,

@@ -97,6 +97,12 @@ def min_blocks(fittype, variant):
     return _native.lib().bsfit_tune_min_blocks(int(fittype), int(variant))
 
 
+def rois_per_warp(fittype, variant):
+    """ROIs a warp fits at once in a variant (2: fit type 6's pair form), 0 if
+    the variant does not exist."""
+    return _native.lib().bsfit_tune_rois_per_warp(int(fittype), int(variant))
+
+
 def current(fittype, roi_size):
     """(variant, warps_per_block) in force on the current device; variant -1
     when the default applies."""
@@ -135,7 +141,8 @@ def autotune(model, rois, iterations, reps=3, cache=None, stream=None):
     cand = {f"v{v}w{w}": (all_ms[v * 3 + i] if all_ms[v * 3 + i] > 0 else None)
             for v in range(nv) for i, w in enumerate(WARPS_PER_BLOCK)}
     choice = {"variant": bv.value, "warps_per_block": bw.value,
-              "min_blocks": min_blocks(model.fittype, bv.value), "ms": bms.value,
+              "min_blocks": min_blocks(model.fittype, bv.value),
+              "rois_per_warp": rois_per_warp(model.fittype, bv.value), "ms": bms.value,
               "candidates": cand}
     if cache is not None:
         c = load_cache(cache)

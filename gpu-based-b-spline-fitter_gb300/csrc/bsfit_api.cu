@@ -53,6 +53,8 @@ int check_coeff(int fittype, int ndim, const int64_t* dims) {
   // The reference indexes X rows with size(coeff, 1) and clamps Y with
   // size(coeff, 2); unequal lateral sizes read outside the array there.
   if (dims[0] != dims[1]) return BSFIT_E_COEFF_SIZE;
+  // offsets within one lateral plane are 32-bit in the kernels
+  if (dims[0] * dims[1] >= (int64_t(1) << 31)) return BSFIT_E_COEFF_SIZE;
   return BSFIT_OK;
 }
 
@@ -1192,6 +1194,11 @@ int bsfit_tune_num_variants(int32_t fittype) { return bsfit::tune_num_variants(f
 
 int bsfit_tune_min_blocks(int32_t fittype, int32_t variant) {
   return bsfit::tune_min_blocks(fittype, variant);
+}
+
+int bsfit_tune_rois_per_warp(int32_t fittype, int32_t variant) {
+  if (variant < 0 || variant >= bsfit::tune_num_variants(fittype)) return 0;
+  return bsfit::tune_rois_per_warp(fittype, variant);
 }
 
 int bsfit_tune_set(int32_t fittype, int64_t roi_size, int32_t variant, int32_t warps_per_block) {

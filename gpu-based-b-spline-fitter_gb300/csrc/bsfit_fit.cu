@@ -102,7 +102,9 @@ cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t 
       tc.variant > 0)
     kern = batch_variant(mode, tc.variant);
   if (!kern) return cudaErrorInvalidValue;
-  const int per_warp = warp_smem_floats(mode, a.s_max, false, tune_staged(mode, tc.variant)) * 4;
+  const int rpw = tune_rois_per_warp(mode, tc.variant);
+  const int per_warp =
+      rpw * warp_smem_floats(mode, a.s_max, false, tune_staged(mode, tc.variant)) * 4;
   int wpb = 4, blocks_per_sm = 0, sms = 0;
   cudaError_t e = pick_launch_wpb((const void*)kern, per_warp, multi ? 0 : tc.wpb, &wpb,
                                   &blocks_per_sm, &sms);
@@ -111,7 +113,7 @@ cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t 
   int64_t total = 0;
   for (int i = 0; i < a.nseg; ++i) total += a.seg[i].n;
   int64_t grid = (int64_t)sms * blocks_per_sm;
-  const int64_t need = (total + wpb - 1) / wpb;
+  const int64_t need = (total + rpw * wpb - 1) / (rpw * wpb);
   if (need < grid) grid = need;
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(a);
@@ -303,14 +305,16 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
       tc.variant > 0)
     kern = fit_variant(mode, tc.variant);
   if (!kern) return cudaErrorInvalidValue;
+  // ROIs per warp: 2 for the pair variants of fit type 6 (two workspaces per warp)
+  const int rpw = tunable ? tune_rois_per_warp(mode, tc.variant) : 1;
   const int per_warp =
-      warp_smem_floats(mode, a.s, var, tunable ? tune_staged(mode, tc.variant) : 0) * 4;
+      rpw * warp_smem_floats(mode, a.s, var, tunable ? tune_staged(mode, tc.variant) : 0) * 4;
   int wpb = 4, blocks_per_sm = 0, sms = 0;
   cudaError_t e = pick_launch_wpb((const void*)kern, per_warp, tunable ? tc.wpb : 0, &wpb,
                                   &blocks_per_sm, &sms);
   if (e != cudaSuccess) return e;
   const int smem = per_warp * wpb;
-  int64_t need = (a.nfits + wpb - 1) / wpb;
+  int64_t need = (a.nfits + rpw * wpb - 1) / (rpw * wpb);
   int64_t grid = (int64_t)sms * blocks_per_sm;
   if (need < grid) grid = need;
   // More ROIs than resident warps: claim them dynamically (iteration counts

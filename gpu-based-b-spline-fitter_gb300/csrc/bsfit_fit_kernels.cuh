@@ -178,7 +178,10 @@ struct WarpLayout {
     return x + ((s - x) % 32 + 32) % 32;
   }
   __host__ __device__ constexpr int as() const { return bank_pad(na * wp, s); }  // A column stride
-  __host__ __device__ constexpr int gp() const { return ng | 1; }               // G item stride
+  // G item stride: odd (bank-conflict-free scalar accesses), or 4 for the 3D
+  // model's three maps, read and written as one 16-byte vector per item (a
+  // quarter-warp's eight consecutive items fill the 32 banks)
+  __host__ __device__ constexpr int gp() const { return ng == 3 ? 4 : (ng | 1); }
   __host__ __device__ constexpr int gs() const { return s * gp(); }             // G column stride
   __host__ __device__ constexpr int off_kx() const { return (nch + nvar) * s2p; }
   __host__ __device__ constexpr int off_ky() const { return off_kx() + ((s + 3) & ~3); }
@@ -194,7 +197,7 @@ struct WarpLayout {
     return (a_rel() + wp * as() > wp * gs()) ? a_rel() + wp * as() : wp * gs();
   }
   __host__ __device__ constexpr int off_stage() const { return off_maps() + maps_size(); }
-  __host__ __device__ constexpr int total() const { return off_stage() + stage; }
+  __host__ __device__ constexpr int total() const { return (off_stage() + stage + 3) & ~3; }
 };
 
 // Staged 5D gathers: two buffers of kStageQ coefficients (the 4 x 4 x 4 (u, w,
@@ -235,7 +238,8 @@ constexpr bool layouts_disjoint() {
           return false;
         for (int c = 0; c < L.wp; ++c)
           if ((c + 1) * L.gs() > L.a_rel() + c * L.as()) return false;
-        if (L.as() < L.na * L.wp || L.gp() < L.ng || (L.as() - s) % 32 != 0 || L.gp() % 2 == 0)
+        if (L.as() < L.na * L.wp || L.gp() < L.ng || (L.as() - s) % 32 != 0 ||
+            (L.gp() % 2 == 0 && L.gp() != 4) || L.total() % 4 != 0 || L.off_g() % 4 != 0)
           return false;
       }
   return true;
@@ -267,15 +271,27 @@ __device__ __forceinline__ int hidx(int l, int m) {
   return l * NV - (l * (l - 1)) / 2 + (m - l);
 }
 
+// floor(a / b) for 0 <= a <= 64 and 1 <= b <= 64 without an integer division:
+// q = trunc(a * r + 2^-10) with r the approximate reciprocal of b (relative
+// error at most 2^-21). When a / b is an integer k <= 64, a * r >= k - 2^-15
+// and the 2^-10 lifts it above k; otherwise a / b <= k + 1 - 1/b with
+// 1/b >= 2^-6, so a * r + 2^-10 < k + 1 - 2^-6 + 2^-15 + 2^-10 < k + 1. The
+// window and ROI widths (at most 55) and lane counts stay in that domain.
+__device__ __forceinline__ int small_div(int a, int b) {
+  const float r = __fdividef(1.0f, (float)b);
+  return __float2int_rz(fmaf((float)a, r, 0.0009765625f));
+}
+
 // Row/column of item t of a row-major (rows x w) grid for a lane that starts at
-// t = lane and advances by 32: avoids a runtime integer division per item.
+// t = lane and advances by `step` (32, or 16 for a half-warp's lanes): avoids a
+// runtime integer division per item.
 struct Stride2D {
   int r, c, dr, dc, w;
-  __device__ __forceinline__ Stride2D(int lane, int w_) : w(w_) {
-    r = lane / w;
+  __device__ __forceinline__ Stride2D(int lane, int w_, int step = 32) : w(w_) {
+    r = small_div(lane, w);
     c = lane - r * w;
-    dr = 32 / w;
-    dc = 32 - dr * w;
+    dr = small_div(step, w);
+    dc = step - dr * w;
   }
   __device__ __forceinline__ void next() {
     r += dr;
@@ -300,11 +316,24 @@ __device__ __forceinline__ float wrap_phase(float w, int nw) {
 // One image channel of one ROI evaluation: model and derivatives at th for
 // every pixel of `data`, accumulated into this lane's partial sums (err, and
 // acc = gradient 0 .. NV-1, packed Hessian or Fisher upper triangle NV ..).
-template <int MODE, int KP, bool VAR, int STG = 0>
+//
+// LW lanes work on the ROI: the whole warp (LW = 32, lane = 0..31, gm = the
+// full mask), or one half of it (LW = 16, lane = 0..15 within the half, gm =
+// the half's mask; the two halves evaluate two ROIs in their own workspaces).
+// Every node, item and pixel is computed by the same operations either way.
+// The per-pixel sums keep the whole warp's order in both forms: with LW = 32
+// lane l sums pixels l, l + 32, l + 64, ... into (err, acc); with LW = 16 lane
+// l sums those pixels into (err, acc) and pixels l + 16, l + 48, ... (the
+// sequence of warp lane l + 16) into (err2, acc2), so the reductions that
+// follow can form the same sums as the whole warp's.
+template <int MODE, int KP, bool VAR, int STG = 0, int LW = 32>
 __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout& L, float* ws,
                                              const float* data, int lane, const float* th,
                                              bool dup45, bool FISHER, FPair& err,
-                                             float (&acc)[KP]) {
+                                             float (&acc)[KP], FPair& err2, float (&acc2)[KP],
+                                             unsigned gm = kFull) {
+  static_assert(LW == 32 || (LW == 16 && MODE == 6 && !VAR && STG == 0),
+                "half-warp ROIs: the 3D EMCCD model only");
   using TR = ModeTraits<MODE>;
   constexpr int D = TR::D;
   constexpr int NV = TR::NV;
@@ -329,7 +358,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
   const float wc = (D >= 4) ? th[5] : 0.0f;
   const float uc = (D >= 5) ? th[6] : 0.0f;
 
-  for (int j = lane; j < s; j += 32) {
+  for (int j = lane; j < s; j += LW) {
     kxs[j] = knot_index((xc + (float)j) + off, m.n[1]);
     kys[j] = knot_index((yc + (float)j) + off, m.n[0]);
   }
@@ -342,7 +371,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     fr[3] = wc - floorf(wc);
     fr[4] = uc - floorf(uc);
     // 7 weights per axis: 35 for the 5D model, more than one per lane.
-    for (int k = lane; k < 7 * D; k += 32) {
+    for (int k = lane; k < 7 * D; k += LW) {
       const int ax = k / 7;
       w[ax * 8 + (k - ax * 7)] = axis_weight(fr[ax], k - ax * 7);
     }
@@ -351,16 +380,16 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
   int kxmin, kxmax, kymin, kymax;
   {
     int a0 = INT_MAX, a1 = INT_MIN, b0 = INT_MAX, b1 = INT_MIN;
-    for (int j = lane; j < s; j += 32) {
+    for (int j = lane; j < s; j += LW) {
       a0 = min(a0, kxs[j]);
       a1 = max(a1, kxs[j]);
       b0 = min(b0, kys[j]);
       b1 = max(b1, kys[j]);
     }
-    kxmin = warp_min(a0);
-    kxmax = warp_max(a1);
-    kymin = warp_min(b0);
-    kymax = warp_max(b1);
+    kxmin = __reduce_min_sync(gm, a0);
+    kxmax = __reduce_max_sync(gm, a1);
+    kymin = __reduce_min_sync(gm, b0);
+    kymax = __reduce_max_sync(gm, b1);
   }
   // Window of lateral nodes [k - 1, k + 2] over all pixels. Its extent is at
   // most s + 4 (the per-pixel knots grow by one per pixel, plus one for
@@ -380,12 +409,18 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     const int64_t sz_ = m.st[2];
     const int nodes = wx * wy;
     if constexpr (D == 3) {
-      const float* base = m.coeff + (int64_t)(kz - 1) * sz_;
-      Stride2D ix(lane, wy);
-      for (int t = lane; t < nodes; t += 32, ix.next()) {
+      // one base pointer per z plane and 32-bit lateral offsets (a 3D table
+      // has far fewer than 2^31 elements)
+      const float* b0 = m.coeff + (int64_t)(kz - 1) * sz_;
+      const float* b1 = b0 + sz_;
+      const float* b2 = b1 + sz_;
+      const float* b3 = b2 + sz_;
+      const int st1 = (int)m.st[1];
+      Stride2D ix(lane, wy, LW);
+      for (int t = lane; t < nodes; t += LW, ix.next()) {
         const int xr = ix.r, yr = ix.c;
-        const float* p = base + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
-        float c0 = __ldg(p), c1 = __ldg(p + sz_), c2 = __ldg(p + 2 * sz_), c3 = __ldg(p + 3 * sz_);
+        const int lat = (xb + xr) * st1 + (yb + yr);
+        float c0 = __ldg(b0 + lat), c1 = __ldg(b1 + lat), c2 = __ldg(b2 + lat), c3 = __ldg(b3 + lat);
         float v = c0 * bz0 + c1 * bz1 + c2 * bz2 + c3 * bz3;
         float dz = (c1 - c0) * dz0 + (c2 - c1) * dz1 + (c3 - c2) * dz2;
         A[xr * AS + yr] = v;
@@ -691,8 +726,11 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     const float dy0 = w[4], dy1 = w[5], dy2 = w[6];
     constexpr int NG = TR::NG;
     const int items = wx * s;
-    Stride2D ix(lane, s);
-    for (int t0 = 0; t0 < items; t0 += 32, ix.next()) {
+    // the two halves' item counts differ with their windows: both run the
+    // larger count, so the synchronisation below is reached by the whole warp
+    const int items_u = (LW == 32) ? items : max(items, __shfl_xor_sync(kFull, items, 16));
+    Stride2D ix(lane, s, LW);
+    for (int t0 = 0; t0 < items_u; t0 += LW, ix.next()) {
       const bool act = t0 + lane < items;
       const int xr = ix.r, py = ix.c;
       float gv[NG];
@@ -729,8 +767,12 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       if constexpr (TR::ALIAS) __syncwarp();  // G aliases A (see WarpLayout)
       if (act) {
         float* go = G + (xr * s + py) * GP;
+        if constexpr (MODE == 6) {
+          *reinterpret_cast<float4*>(go) = make_float4(gv[0], gv[1], gv[2], 0.0f);
+        } else {
 #pragma unroll
-        for (int c = 0; c < NG; ++c) go[c] = gv[c];
+          for (int c = 0; c < NG; ++c) go[c] = gv[c];
+        }
       }
     }
   }
@@ -743,22 +785,36 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     const float dx0 = w[12], dx1 = w[13], dx2 = w[14];
     const float N = th[2], bg = th[3];
     const int s2 = s * s;
-    Stride2D ix(lane, s);
-    for (int p = lane; p < s2; p += 32, ix.next()) {
-      const int px = ix.r, py = ix.c;  // px = jj (X), py = ii (Y)
+    // pixel p = px * s + py, px = jj (X), py = ii (Y), into the chain (er, ac)
+    auto pixel = [&](int p, int px, int py, FPair& er, float (&ac)[KP]) {
       int ox = min(max(kxs[px] - 1 - xb, 0), wx - 4);
       const float* g = G + (ox * s + py) * GP;  // X node k of map c at g[k * GS + c]
+      float dudt[NV];
+      float model;
+      if constexpr (MODE == 6) {
+        // the item's three maps as one vector per X node (value, d/dY, d/dz)
+        const float4* g4 = reinterpret_cast<const float4*>(g);
+        const float4 q0 = g4[0], q1 = g4[s], q2 = g4[2 * s], q3 = g4[3 * s];
+        float f = q0.x * bx0 + q1.x * bx1 + q2.x * bx2 + q3.x * bx3;
+        float dX = (q1.x - q0.x) * dx0 + (q2.x - q1.x) * dx1 + (q3.x - q2.x) * dx2;
+        float dY = q0.y * bx0 + q1.y * bx1 + q2.y * bx2 + q3.y * bx3;
+        float dc = q0.z * bx0 + q1.z * bx1 + q2.z * bx2 + q3.z * bx3;
+        dudt[0] = -N * dX;
+        dudt[1] = -N * dY;
+        dudt[2] = f;
+        dudt[3] = 1.0f;
+        dudt[4] = N * dc;
+        model = bg + N * f;
+      } else {
       float g0 = g[0], g1 = g[GS], g2 = g[2 * GS], g3 = g[3 * GS];
       float f = g0 * bx0 + g1 * bx1 + g2 * bx2 + g3 * bx3;
       float dX = (g1 - g0) * dx0 + (g2 - g1) * dx1 + (g3 - g2) * dx2;
       const float* gy = g + 1;
       float dY = gy[0] * bx0 + gy[GS] * bx1 + gy[2 * GS] * bx2 + gy[3 * GS] * bx3;
-      float dudt[NV];
       dudt[0] = -N * dX;
       dudt[1] = -N * dY;
       dudt[2] = f;
       dudt[3] = 1.0f;
-      float model;
       if constexpr (MODE != 8) {
 #pragma unroll
         for (int c = 1; c < TR::NA; ++c) {
@@ -803,6 +859,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         dudt[NV - 1] = N * (f - f3);
         model = m3 * h2m + m5 * g2;
       }
+      }
       float d = data[p];
       if constexpr (VAR) {
         // sCMOS: variance / gain^2 added to model and data
@@ -823,17 +880,17 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         } else {
           term = 2.0f * model;
         }
-        err.add(term);
+        er.add(term);
         const float t1 = 1.0f - dm;
         const float t2 = dm * inv;
 #pragma unroll
-        for (int l = 0; l < NV; ++l) acc[l] = fmaf(t1, dudt[l], acc[l]);
+        for (int l = 0; l < NV; ++l) ac[l] = fmaf(t1, dudt[l], ac[l]);
         int k = NV;
 #pragma unroll
         for (int l = 0; l < NV; ++l) {
           const float tl = t2 * dudt[l];
 #pragma unroll
-          for (int mm = l; mm < NV; ++mm, ++k) acc[k] = fmaf(tl, dudt[mm], acc[k]);
+          for (int mm = l; mm < NV; ++mm, ++k) ac[k] = fmaf(tl, dudt[mm], ac[k]);
         }
       } else {
         // Fisher information and log-likelihood (CPUmleFit_LM.cpp:2730-2742).
@@ -843,12 +900,22 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         for (int l = 0; l < NV; ++l) {
           const float tl = dudt[l] * im;
 #pragma unroll
-          for (int mm = l; mm < NV; ++mm, ++k) acc[k] = fmaf(tl, dudt[mm], acc[k]);
+          for (int mm = l; mm < NV; ++mm, ++k) ac[k] = fmaf(tl, dudt[mm], ac[k]);
         }
         if (model > 0.0f) {
           float ll = (d > 0.0f) ? (d * logf(model) - model - d * logf(d) + d) : -model;
-          err.add(ll);
+          er.add(ll);
         }
+      }
+    };
+    if constexpr (LW == 32) {
+      Stride2D ix(lane, s);
+      for (int p = lane; p < s2; p += 32, ix.next()) pixel(p, ix.r, ix.c, err, acc);
+    } else {
+      Stride2D ia(lane, s), ib(lane + 16, s);
+      for (int p = lane; p < s2; p += 32, ia.next(), ib.next()) {
+        pixel(p, ia.r, ia.c, err, acc);
+        if (p + 16 < s2) pixel(p + 16, ib.r, ib.c, err2, acc2);
       }
     }
   }
@@ -871,7 +938,7 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
 #pragma unroll
   for (int k = 0; k < KP; ++k) acc[k] = 0.0f;
   if constexpr (TR::NCH == 1) {
-    channel_pass<MODE, KP, VAR, STG>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc);
+    channel_pass<MODE, KP, VAR, STG>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc, err, acc);
   } else {
     // 4Pi: channel c sees the shared parameters plus its offsets dT[c], with
     // its phase shifted by shift[c] and wrapped; the sums run over all
@@ -882,7 +949,8 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
 #pragma unroll
       for (int k = 0; k < NV; ++k) thc[k] = th[k] + dts[ch * NV + k];
       thc[5] = wrap_phase(thc[5] + a.m.shift[ch], a.m.n[3]);
-      channel_pass<MODE, KP, VAR>(a, L, ws, ws + ch * L.s2p, lane, thc, false, FISHER, err, acc);
+      channel_pass<MODE, KP, VAR>(a, L, ws, ws + ch * L.s2p, lane, thc, false, FISHER, err, acc, err,
+                                  acc);
     }
   }
   PHASE_DECL();

@@ -186,6 +186,8 @@ int tune_min_blocks(int mode, int variant);
 // 1 when the variant stages the 5D gathers through shared memory (its
 // per-warp shared memory includes the staging buffers)
 int tune_staged(int mode, int variant);
+// ROIs fitted per warp by a variant (2: the half-warp pair form of fit type 6)
+int tune_rois_per_warp(int mode, int variant);
 FitKern fit_variant(int mode, int variant);     // variant >= 1
 BatchKern batch_variant(int mode, int variant);  // variant >= 1
 bool tune_lookup(int mode, int s, int dev, TuneConfig* out);

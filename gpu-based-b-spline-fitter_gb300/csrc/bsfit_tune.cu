@@ -11,7 +11,10 @@
 //    shared memory (ROI pixels and maps, growing with the ROI size) packs into
 //    the SM's shared memory;
 //  - for fit type 8, the staging of stage A's gathers: into registers, or into
-//    shared memory with asynchronous copies one round of 32 nodes ahead.
+//    shared memory with asynchronous copies one round of 32 nodes ahead;
+//  - for fit type 6, the ROIs per warp: one (32 lanes per ROI), or two (one per
+//    half-warp, bsfit_pair.cuh), which shares the per-evaluation work that does
+//    not grow with the ROI between two ROIs at twice the shared memory per warp.
 // Variant 0 is the default kernel (bsfit_fit.cu); this file instantiates the
 // others. Every variant runs the same code, so results are bit-identical
 // across configurations. A table per (fit type, ROI size, device) holds the
@@ -19,12 +22,15 @@
 #include <mutex>
 
 #include "bsfit_fit_kernels.cuh"
+#include "bsfit_pair.cuh"
 
 namespace bsfit {
 
 namespace {
 
-constexpr int kMinBlocks6[3] = {BSFIT_MINBLOCKS(6), 5, 4};
+// fit type 6: variants 3 to 5 fit two ROIs per warp
+constexpr int kMinBlocks6[6] = {BSFIT_MINBLOCKS(6), 5, 4, 6, 5, 4};
+constexpr int kRoisPerWarp6[6] = {1, 1, 1, 2, 2, 2};
 constexpr int kMinBlocks7[3] = {BSFIT_MINBLOCKS(7), 3, 5};
 // fit type 8: variants 2 and 3 stage the 5D gathers through shared memory
 // (cp.async, two rounds of 32 nodes in flight per warp)
@@ -42,7 +48,11 @@ int g_ntune = 0;
 
 }  // namespace
 
-int tune_num_variants(int mode) { return mode == 6 ? 3 : mode == 7 ? 3 : mode == 8 ? 4 : 0; }
+int tune_num_variants(int mode) { return mode == 6 ? 6 : mode == 7 ? 3 : mode == 8 ? 4 : 0; }
+
+int tune_rois_per_warp(int mode, int variant) {
+  return (mode == 6 && variant >= 0 && variant < 6) ? kRoisPerWarp6[variant] : 1;
+}
 
 int tune_staged(int mode, int variant) {
   return (mode == 8 && variant >= 0 && variant < 4 && kStaged8[variant]) ? 1 : 0;
@@ -57,6 +67,9 @@ FitKern fit_variant(int mode, int variant) {
   switch (mode * 10 + variant) {
     case 61: return fit_kernel<6, false, false, kMinBlocks6[1]>;
     case 62: return fit_kernel<6, false, false, kMinBlocks6[2]>;
+    case 63: return fit_pair_kernel<kMinBlocks6[3]>;
+    case 64: return fit_pair_kernel<kMinBlocks6[4]>;
+    case 65: return fit_pair_kernel<kMinBlocks6[5]>;
     case 71: return fit_kernel<7, false, false, kMinBlocks7[1]>;
     case 72: return fit_kernel<7, false, false, kMinBlocks7[2]>;
     case 81: return fit_kernel<8, false, false, kMinBlocks8[1]>;
@@ -70,6 +83,9 @@ BatchKern batch_variant(int mode, int variant) {
   switch (mode * 10 + variant) {
     case 61: return batch_kernel<6, false, kMinBlocks6[1]>;
     case 62: return batch_kernel<6, false, kMinBlocks6[2]>;
+    case 63: return batch_pair_kernel<kMinBlocks6[3]>;
+    case 64: return batch_pair_kernel<kMinBlocks6[4]>;
+    case 65: return batch_pair_kernel<kMinBlocks6[5]>;
     case 71: return batch_kernel<7, false, kMinBlocks7[1]>;
     case 72: return batch_kernel<7, false, kMinBlocks7[2]>;
     case 81: return batch_kernel<8, false, kMinBlocks8[1]>;

@@ -46,8 +46,9 @@ typedef enum bsfit_status {
   BSFIT_E_CUDA = 7,
   /* GPUmleFit_LM:NoDevice / nodevices (mex :186-203) */
   BSFIT_E_NO_DEVICE = 8,
-  /* coefficient array too small (< 5 along an axis), wrong rank, or lateral
-   * sizes unequal (the reference indexes past the array there) */
+  /* coefficient array too small (< 5 along an axis) or too large (> 2^20
+   * along an axis, 2^31 or more elements per lateral plane), wrong rank, or
+   * lateral sizes unequal (the reference indexes past the array there) */
   BSFIT_E_COEFF_SIZE = 9,
   /* initP missing or too short for fit types 7 and 8 (the reference
    * dereferences it, or leaves g2 uninitialised) */
@@ -353,13 +354,15 @@ int bsfit_batch_fit_device_static(const bsfit_segment* segs, int32_t nseg, void*
  * The FP32 fit kernels of fit types 6, 7, 8 (single start, EMCCD; plain and
  * batched) have a launch configuration per fit type, ROI size and device: the
  * kernel variant (its minimum resident 4-warp blocks per SM, which sets the
- * register budget: bsfit_tune_min_blocks) and the warps per block (4, 2 or 1;
- * 0 keeps the occupancy choice). Variant 0 with 0 warps per block is the
+ * register budget: bsfit_tune_min_blocks; for fit type 6 also the ROIs per
+ * warp, one or two: bsfit_tune_rois_per_warp) and the warps per block (4, 2 or
+ * 1; 0 keeps the occupancy choice). Variant 0 with 0 warps per block is the
  * default. Every configuration gives bit-identical results. The batched form
  * uses the configuration of its largest ROI size.
  */
 int bsfit_tune_num_variants(int32_t fittype);                  /* 0 if none */
 int bsfit_tune_min_blocks(int32_t fittype, int32_t variant);   /* 0 if out of range */
+int bsfit_tune_rois_per_warp(int32_t fittype, int32_t variant); /* 0 if out of range */
 /* Sets the configuration for (fittype, roi_size) on the current device;
  * variant -1 restores the default. */
 int bsfit_tune_set(int32_t fittype, int64_t roi_size, int32_t variant, int32_t warps_per_block);

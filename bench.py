@@ -564,7 +564,7 @@ def bench_gpu(args):
         for g, r in zip(groups, d_rois):
             ch = T.autotune(models[id(g.coeff)], r[:args.tune_rois], g.iterations, reps=2)
             tuned[str(g.roi_size)] = {k: ch[k] for k in ("variant", "warps_per_block",
-                                                        "min_blocks", "ms")}
+                                                        "min_blocks", "rois_per_warp", "ms")}
 
     # Batched form: one persistent launch over all size groups per step (the
     # plain form, one call per size group, is timed beside it below).

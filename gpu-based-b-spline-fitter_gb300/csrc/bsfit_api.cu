@@ -53,8 +53,9 @@ int check_coeff(int fittype, int ndim, const int64_t* dims) {
   // The reference indexes X rows with size(coeff, 1) and clamps Y with
   // size(coeff, 2); unequal lateral sizes read outside the array there.
   if (dims[0] != dims[1]) return BSFIT_E_COEFF_SIZE;
-  // offsets within one lateral plane are 32-bit in the kernels
-  if (dims[0] * dims[1] >= (int64_t(1) << 31)) return BSFIT_E_COEFF_SIZE;
+  // offsets spanning a lateral node and up to three z planes are 32-bit in the
+  // kernels
+  if (dims[0] * dims[1] >= (int64_t(1) << 29)) return BSFIT_E_COEFF_SIZE;
   return BSFIT_OK;
 }
 

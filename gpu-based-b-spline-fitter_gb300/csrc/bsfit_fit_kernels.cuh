@@ -409,8 +409,8 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     const int64_t sz_ = m.st[2];
     const int nodes = wx * wy;
     if constexpr (D == 3) {
-      // one base pointer per z plane and 32-bit lateral offsets (a 3D table
-      // has far fewer than 2^31 elements)
+      // one base pointer per z plane and 32-bit lateral offsets (lateral
+      // planes hold fewer than 2^29 elements)
       const float* b0 = m.coeff + (int64_t)(kz - 1) * sz_;
       const float* b1 = b0 + sz_;
       const float* b2 = b1 + sz_;
@@ -431,19 +431,30 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       const float bw[4] = {ww[0], ww[1], ww[2], ww[3]};
       const float dw[3] = {ww[4], ww[5], ww[6]};
       const int64_t sw_ = m.st[3];
-      const float* base = m.coeff + (int64_t)(kz - 1) * sz_ + (int64_t)(kw - 1) * sw_;
+      // one base pointer per w layer and 32-bit offsets within it (the lateral
+      // node plus up to three z planes: lateral planes hold fewer than 2^29
+      // elements)
+      // (fit type 7; the 4Pi kernel keeps 64-bit addressing, which measured
+      // faster within its register budget)
+      const float* pw[4];
+      pw[0] = m.coeff + (int64_t)(kz - 1) * sz_ + (int64_t)(kw - 1) * sw_;
+#pragma unroll
+      for (int iw = 1; iw < 4; ++iw) pw[iw] = pw[iw - 1] + sw_;
+      const int st1 = (int)m.st[1], sz32 = (int)sz_;
       Stride2D ix(lane, wy);
       const float2 BZ0 = bc2(bz0), BZ1 = bc2(bz1), BZ2 = bc2(bz2), BZ3 = bc2(bz3);
       const float2 DZ0 = bc2(dz0), DZ1 = bc2(dz1), DZ2 = bc2(dz2);
       for (int t = lane; t < nodes; t += 32, ix.next()) {
         const int xr = ix.r, yr = ix.c;
-        const float* p = base + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
+        const int o0 = (xb + xr) * st1 + (yb + yr);
+        const int o1 = o0 + sz32, o2 = o1 + sz32, o3 = o2 + sz32;
         // z contraction of the four w layers: two layers per packed operation
         // (fit type 7), or one at a time where the packed operands would push
         // the kernel past its register budget (4Pi, four channels); both
         // orders of operations are the same.
         float vz[4], dzv[4];
         if constexpr (MODE == kFit4Pi) {
+          const float* p = pw[0] + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
 #pragma unroll
           for (int iw = 0; iw < 4; ++iw) {
             const float* q = p + iw * sw_;
@@ -454,12 +465,12 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         } else {
 #pragma unroll
           for (int ip = 0; ip < 2; ++ip) {
-            const float* q0 = p + (2 * ip) * sw_;
-            const float* q1 = q0 + sw_;
-            const float2 c0 = make_float2(__ldg(q0), __ldg(q1));
-            const float2 c1 = make_float2(__ldg(q0 + sz_), __ldg(q1 + sz_));
-            const float2 c2 = make_float2(__ldg(q0 + 2 * sz_), __ldg(q1 + 2 * sz_));
-            const float2 c3 = make_float2(__ldg(q0 + 3 * sz_), __ldg(q1 + 3 * sz_));
+            const float* q0 = pw[2 * ip];
+            const float* q1 = pw[2 * ip + 1];
+            const float2 c0 = make_float2(__ldg(q0 + o0), __ldg(q1 + o0));
+            const float2 c1 = make_float2(__ldg(q0 + o1), __ldg(q1 + o1));
+            const float2 c2 = make_float2(__ldg(q0 + o2), __ldg(q1 + o2));
+            const float2 c3 = make_float2(__ldg(q0 + o3), __ldg(q1 + o3));
             const float2 v2 = contract4x2(c0, c1, c2, c3, BZ0, BZ1, BZ2, BZ3);
             const float2 d2 = dcontract4x2(c0, c1, c2, c3, DZ0, DZ1, DZ2);
             vz[2 * ip] = v2.x;

@@ -47,7 +47,7 @@ typedef enum bsfit_status {
   /* GPUmleFit_LM:NoDevice / nodevices (mex :186-203) */
   BSFIT_E_NO_DEVICE = 8,
   /* coefficient array too small (< 5 along an axis) or too large (> 2^20
-   * along an axis, 2^31 or more elements per lateral plane), wrong rank, or
+   * along an axis, 2^29 or more elements per lateral plane), wrong rank, or
    * lateral sizes unequal (the reference indexes past the array there) */
   BSFIT_E_COEFF_SIZE = 9,
   /* initP missing or too short for fit types 7 and 8 (the reference

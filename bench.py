@@ -145,7 +145,9 @@ def bench_kernel_only(args):
     of 17 px; --model 4pi: the 4Pi fit of --rois ROIs of four 13 px channels;
     --model 3d64: the FP64 reference-precision kernel on --rois 3D ROIs of 13 px;
     --model 4d: fit type 7 on --rois ROIs of 13 px. --precision parity runs the
-    double-float kernels on the 3D (13 px), 4D and 5D cases."""
+    double-float kernels on the 3D (13 px), 4D and 5D cases. 3D only: --variant
+    V --wpb W forces a tuner configuration (e.g. the two-ROIs-per-warp variants
+    3 to 5); --eval runs the evaluation kernel alone, at the fitted parameters."""
     import torch
     import bsfit
     from bsfit import workloads as W
@@ -213,6 +215,11 @@ def bench_kernel_only(args):
                           "launches": launches}))
         return 0
     groups = make_workload(args.rois, tuple(args.sizes))
+    if args.variant is not None:
+        # a forced launch configuration (the tuner's variant and warps per block)
+        from bsfit import tuning as T
+        for g in groups:
+            T._set(6, g.roi_size, args.variant, args.wpb)
     work = []
     for g in groups:
         m = bsfit.Model(6, g.coeff)
@@ -220,6 +227,21 @@ def bench_kernel_only(args):
         o = (torch.empty((6, len(g.rois)), device=dev), torch.empty((5, len(g.rois)), device=dev),
              torch.empty((len(g.rois),), device=dev))
         work.append((m, r, o, g))
+    if args.eval:
+        # the evaluation kernel alone: one untimed fit per size group, then
+        # launches of one evaluation per ROI at the fitted parameters
+        with torch.cuda.stream(stream):
+            ths = []
+            for m, r, o, g in work:
+                m.fit_torch(r, g.iterations, out=o, stream=stream)
+                ths.append(o[0][:5].contiguous())
+            for _ in range(launches):
+                for (m, r, o, g), th in zip(work, ths):
+                    m.eval_torch(r, th, stream=stream)
+        stream.synchronize()
+        print(json.dumps({"profile_case": True, "eval": True, "rois": sum(len(g.rois) for g in groups),
+                          "sizes": args.sizes, "launches": launches * len(work)}))
+        return 0
     batch = bsfit.Batch([(m, r, g.iterations) for m, r, o, g in work]) if args.batched else None
     with torch.cuda.stream(stream):
         for _ in range(launches):
@@ -908,6 +930,11 @@ def main():
                     help="profiling case: only the fit launches of --rois ROIs of --sizes")
     ap.add_argument("--rois", type=int, default=N_ROIS)
     ap.add_argument("--batched", action="store_true", help="kernel-only: the batched form")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="kernel-only, 3D: force this tuner variant (with --wpb warps per block)")
+    ap.add_argument("--wpb", type=int, default=0, help="kernel-only: warps per block with --variant")
+    ap.add_argument("--eval", action="store_true",
+                    help="kernel-only, 3D: the evaluation kernel at the fitted parameters")
     ap.add_argument("--model", default="3d", choices=["3d", "4d", "5d", "4pi", "3d64"],
                     help="kernel-only: model")
     ap.add_argument("--sizes", type=int, nargs="+", default=list(SIZES))

@@ -131,11 +131,11 @@ class ClockSampler:
                 "samples": len(self.samples), "period_ms": self.PERIOD_MS}
 
 
-def make_workload(n=N_ROIS, sizes=SIZES):
+def make_workload(n=N_ROIS, sizes=SIZES, iterations=ITERATIONS):
     from bsfit import workloads as W
     if len(sizes) == 1:
-        return [W.workload_3d(n, s=sizes[0], iterations=ITERATIONS, stream=2)]
-    return W.workload_3d_mixed(n, sizes=sizes, ratio=(1, 2, 1), iterations=ITERATIONS)
+        return [W.workload_3d(n, s=sizes[0], iterations=iterations, stream=2)]
+    return W.workload_3d_mixed(n, sizes=sizes, ratio=(1, 2, 1), iterations=iterations)
 
 
 def bench_kernel_only(args):
@@ -214,7 +214,7 @@ def bench_kernel_only(args):
         print(json.dumps({"profile_case": True, "model": "4pi", "rois": w4.n_fits,
                           "launches": launches}))
         return 0
-    groups = make_workload(args.rois, tuple(args.sizes))
+    groups = make_workload(args.rois, tuple(args.sizes), args.iterations)
     if args.variant is not None:
         # a forced launch configuration (the tuner's variant and warps per block)
         from bsfit import tuning as T
@@ -933,6 +933,8 @@ def main():
     ap.add_argument("--variant", type=int, default=None,
                     help="kernel-only, 3D: force this tuner variant (with --wpb warps per block)")
     ap.add_argument("--wpb", type=int, default=0, help="kernel-only: warps per block with --variant")
+    ap.add_argument("--iterations", type=int, default=ITERATIONS,
+                    help="kernel-only, 3D: the LM iteration cap (0: initial and CRLB passes only)")
     ap.add_argument("--eval", action="store_true",
                     help="kernel-only, 3D: the evaluation kernel at the fitted parameters")
     ap.add_argument("--model", default="3d", choices=["3d", "4d", "5d", "4pi", "3d64"],

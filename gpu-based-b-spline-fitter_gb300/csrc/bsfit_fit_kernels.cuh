@@ -331,7 +331,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
                                              const float* data, int lane, const float* th,
                                              bool dup45, bool FISHER, FPair& err,
                                              float (&acc)[KP], FPair& err2, float (&acc2)[KP],
-                                             unsigned gm = kFull) {
+                                             unsigned gm = kFull, bool maps_ready = false) {
   static_assert(LW == 32 || (LW == 16 && MODE == 6 && !VAR && STG == 0),
                 "half-warp ROIs: the 3D EMCCD model only");
   using TR = ModeTraits<MODE>;
@@ -396,13 +396,24 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
   // rounding); the caps keep every shared-memory access inside the warp's maps.
   const int xb = kxmin - 1, wx = min(kxmax - kxmin + 4, wp);
   const int yb = kymin - 1, wy = min(kymax - kymin + 4, wp);
+  // Per pixel row: the window offset of its first Y node (clamped so the four
+  // reads stay in the window); per pixel column: that of its first X node,
+  // times the G column stride. Written over the knots by the lane that read
+  // them; stages B and C read them after the synchronisation that ends stage A.
+  for (int j = lane; j < s; j += LW) {
+    kxs[j] = min(max(kxs[j] - 1 - xb, 0), wx - 4) * GS;
+    kys[j] = min(max(kys[j] - 1 - yb, 0), wy - 4);
+  }
   const int kz = knot_index(zc, m.n[2]);
   const int kw = (D >= 4) ? knot_index(wc, m.n[3]) : 0;
   const int ku = (D >= 5) ? knot_index(uc, m.n[4]) : 0;
   PHASE_MARK(0);
 
-  // (A) Non-lateral contraction at every lateral node of the window.
-  {
+  // (A) Non-lateral contraction at every lateral node of the window. Skipped
+  // with maps_ready: the caller guarantees that the maps in the workspace were
+  // made by the previous evaluation at the same spatial parameters, so they
+  // hold exactly the values these two stages would write.
+  if (!maps_ready) {
     const float* wz = w + 2 * 8;
     const float bz0 = wz[0], bz1 = wz[1], bz2 = wz[2], bz3 = wz[3];
     const float dz0 = wz[4], dz1 = wz[5], dz2 = wz[6];
@@ -732,7 +743,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
   // (B) Y contraction for every (X node, pixel row ii), column by column. Where
   // G is written over the A columns already read (the layout's aliasing rule),
   // every pass of the warp reads its A values, synchronises, then writes.
-  {
+  if (!maps_ready) {
     const float by0 = w[0], by1 = w[1], by2 = w[2], by3 = w[3];
     const float dy0 = w[4], dy1 = w[5], dy2 = w[6];
     constexpr int NG = TR::NG;
@@ -746,7 +757,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       const int xr = ix.r, py = ix.c;
       float gv[NG];
       if (act) {
-        const int oy = min(max(kys[py] - 1 - yb, 0), wy - 4);
+        const int oy = kys[py];
         const float* a0 = A + xr * AS + oy;
         const float v0 = a0[0], v1 = a0[1], v2 = a0[2], v3 = a0[3];
         gv[0] = v0 * by0 + v1 * by1 + v2 * by2 + v3 * by3;
@@ -798,8 +809,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     const int s2 = s * s;
     // pixel p = px * s + py, px = jj (X), py = ii (Y), into the chain (er, ac)
     auto pixel = [&](int p, int px, int py, FPair& er, float (&ac)[KP]) {
-      int ox = min(max(kxs[px] - 1 - xb, 0), wx - 4);
-      const float* g = G + (ox * s + py) * GP;  // X node k of map c at g[k * GS + c]
+      const float* g = G + (kxs[px] + py * GP);  // X node k of map c at g[k * GS + c]
       float dudt[NV];
       float model;
       if constexpr (MODE == 6) {
@@ -935,10 +945,12 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
 
 // Outputs are distributed over the lanes: lane l < NV receives gradient entry
 // l (gl) and Hessian row l (hr), or Fisher row l; err_out is on every lane.
+// maps_ready (single-channel models): the workspace still holds the maps of the
+// previous evaluation, made at the same spatial parameters (see channel_pass).
 template <int MODE, bool VAR = false, int STG = 0>
 __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int lane,
                          const float* th, bool dup45, bool FISHER, FPair& err_out, float& gl,
-                         float (&hr)[ModeTraits<MODE>::NV]) {
+                         float (&hr)[ModeTraits<MODE>::NV], bool maps_ready = false) {
   using TR = ModeTraits<MODE>;
   constexpr int NV = TR::NV;
   constexpr int NH = NV * (NV + 1) / 2;
@@ -949,7 +961,8 @@ __device__ void evaluate(const FitArgs& a, const WarpLayout& L, float* ws, int l
 #pragma unroll
   for (int k = 0; k < KP; ++k) acc[k] = 0.0f;
   if constexpr (TR::NCH == 1) {
-    channel_pass<MODE, KP, VAR, STG>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc, err, acc);
+    channel_pass<MODE, KP, VAR, STG>(a, L, ws, ws, lane, th, dup45, FISHER, err, acc, err, acc,
+                                     kFull, maps_ready);
   } else {
     // 4Pi: channel c sees the shared parameters plus its offsets dT[c], with
     // its phase shifted by shift[c] and wrapped; the sums run over all
@@ -1268,12 +1281,26 @@ __device__ RoiResult fit_roi(const FitArgs& a, const WarpLayout& L, float* ws, i
       // Parameters of the evaluation, broadcast to every lane. Fit type 8's
       // CRLB pass keeps the positions and g2 of the last evaluation
       // (CPUmleFit_LM.cpp:3568-3584) with the current N and bg.
+      // The maps of stages A and B depend on the spatial parameters only (not
+      // on N, bg or g2). The CRLB pass usually evaluates at the position of
+      // the last evaluation (after the stop test, or at the iteration cap after
+      // an accepted step; fit type 8 by construction): it then reuses that
+      // evaluation's maps, which are still in the workspace, and runs stage C
+      // alone. After a rejected step the position differs and the pass is
+      // complete. Bitwise equality, so the results are those of a full pass.
+      bool maps_ready = false;
+      if (fisher && TR::NCH == 1) {
+        const bool spatial = lane < NV && lane != 2 && lane != 3 && !(MODE == 8 && lane == 7);
+        const bool same = (MODE == 8) || !spatial || __float_as_uint(par) == __float_as_uint(par_eval);
+        maps_ready = __all_sync(kFull, same);
+      }
       if (!fisher) par_eval = par;
       float the[NV];
 #pragma unroll
       for (int k = 0; k < NV; ++k)
         the[k] = bcast((MODE == 8 && fisher && k != 2 && k != 3) ? par_eval : par, k);
-      evaluate<MODE, VAR, STG>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr);
+      evaluate<MODE, VAR, STG>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr,
+                               maps_ready);
       first = false;
       need_eval = false;
       if (fisher) {

@@ -24,6 +24,7 @@ struct bsfit_model_s {
   ModelDev dev;
   float* d_coeff = nullptr;
   float* d_coeff3 = nullptr;
+  float4* d_zq = nullptr;  // stage-A gather table of the FP32 kernels (fit type 7, 4Pi)
   // Double copies for the FP64 reference-precision fit, made on first use.
   double* d_coeff64 = nullptr;
   double* d_coeff3_64 = nullptr;
@@ -92,6 +93,19 @@ int cuda_status(cudaError_t e) {
   if (e == cudaErrorMemoryAllocation) return BSFIT_E_NOT_ENOUGH_MEMORY;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return BSFIT_E_NO_DEVICE;
   return BSFIT_E_CUDA;
+}
+
+// The stage-A gather table of a model whose coefficients are on the device:
+// allocated, built on the legacy default stream and waited for, so that fits
+// on any stream see it.
+cudaError_t make_zq(bsfit_model_s* m) {
+  const int64_t n = bsfit::zq_entries(m->dev);
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e = cudaMalloc(&m->d_zq, (size_t)n * sizeof(float4));
+  if (e == cudaSuccess) e = bsfit::build_zq(m->dev, m->d_zq, nullptr);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
+  if (e == cudaSuccess) bsfit::set_zq(m->dev, m->d_zq);
+  return e;
 }
 
 // Argument checks of a model (shared by bsfit_model_create and the drop-in
@@ -247,6 +261,14 @@ int bsfit_model_create(int32_t fittype, const float* coeff, int32_t coeff_ndim,
   }
   m->dev.coeff = m->d_coeff;
   m->dev.coeff3 = m->d_coeff3;
+  e = make_zq(m);
+  if (e != cudaSuccess) {
+    cudaFree(m->d_coeff);
+    cudaFree(m->d_coeff3);
+    cudaFree(m->d_zq);
+    delete m;
+    return cuda_status(e);
+  }
   *out = m;
   return BSFIT_OK;
 }
@@ -257,6 +279,7 @@ int bsfit_model_release(bsfit_model model) {
   if (!model) return BSFIT_E_INVALID;
   cudaFree(model->d_coeff);
   cudaFree(model->d_coeff3);
+  cudaFree(model->d_zq);
   cudaFree(model->d_coeff64);
   cudaFree(model->d_coeff3_64);
   delete model;
@@ -510,6 +533,7 @@ int multid_call(const float* imstack, int64_t roi_size, int64_t roi_size2, int64
     cb[nchunk] = nfits;
   }
   float *d_rois = nullptr, *d_out = nullptr, *d_c = nullptr, *d_c3 = nullptr;
+  float4* d_zq = nullptr;
   cudaError_t e = cudaMallocAsync(&d_rois, in_bytes, cp);
   if (e == cudaSuccess) e = cudaMallocAsync(&d_out, out_bytes, cp);
   if (e == cudaSuccess) e = cudaMallocAsync(&d_c, c_bytes, cp);
@@ -522,6 +546,12 @@ int multid_call(const float* imstack, int64_t roi_size, int64_t roi_size2, int64
   fill_model(a.m, fittype, coeff_dims, init_p, init_p_numel);
   a.m.coeff = d_c;
   a.m.coeff3 = d_c3;
+  // the stage-A gather table, built on the copy stream after the upload (every
+  // chunk's fit waits for an event recorded on that stream after it)
+  const int64_t zq_n = bsfit::zq_entries(a.m);
+  if (e == cudaSuccess && zq_n > 0) e = cudaMallocAsync(&d_zq, (size_t)zq_n * sizeof(float4), cp);
+  if (e == cudaSuccess && zq_n > 0) e = bsfit::build_zq(a.m, d_zq, cp);
+  bsfit::set_zq(a.m, d_zq);
   a.s = (int)roi_size;
   a.iterations = iterations;
   a.P = d_out;
@@ -572,6 +602,7 @@ int multid_call(const float* imstack, int64_t roi_size, int64_t roi_size2, int64
   if (d_out) cudaFreeAsync(d_out, c0);
   if (d_c) cudaFreeAsync(d_c, c0);
   if (d_c3) cudaFreeAsync(d_c3, c0);
+  if (d_zq) cudaFreeAsync(d_zq, c0);
   cudaError_t e2 = cudaStreamSynchronize(c0);
   if (e == cudaSuccess) e = e2;
   return cuda_status(e);
@@ -623,6 +654,13 @@ int bsfit_model_create_4pi(const float* coeff, int32_t coeff_ndim, const int64_t
     return cuda_status(e);
   }
   m->dev.coeff = m->d_coeff;
+  e = make_zq(m);
+  if (e != cudaSuccess) {
+    cudaFree(m->d_coeff);
+    cudaFree(m->d_zq);
+    delete m;
+    return cuda_status(e);
+  }
   *out = m;
   return BSFIT_OK;
 }

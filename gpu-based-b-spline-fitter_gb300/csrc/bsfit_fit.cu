@@ -8,6 +8,76 @@
 
 namespace bsfit {
 
+// ---------------------------------------------------------------------------
+// Stage-A gather table (ModelDev::zq). Entry i of a table with P lateral
+// nodes per plane and nq = n[2] z knots (knot k = 1 .. n[2] reads planes
+// k - 1 .. k + 2):
+//   4Pi: i = (wi * nq + kq) * P + lat holds planes kq .. kq + 3 of w layer wi
+//     at lateral node lat;
+//   fit type 7: i = ((wi * nq + kq) * 2 + h) * P + lat holds planes kq + 2h and
+//     kq + 2h + 1 of layers wi and wi + 1, as (plane 0 layer wi, plane 0 layer
+//     wi + 1, plane 1 layer wi, plane 1 layer wi + 1), for first layers
+//     wi = 0 .. nW - 2 (the kernel pairs w layers kw - 1, kw and kw + 1, kw + 2).
+// Every read stays inside the table: kq + 3 <= n[2] + 2 = nZ - 1, wi + 1 <= nW - 1.
+// The 3D kernels read the coefficient table itself (a table of this kind
+// measured no faster there) and the 5D one would not stay L2-resident at 4x
+// its 56 MB.
+
+__global__ void build_zq_kernel(const float* __restrict__ c, float4* __restrict__ q,
+                                int64_t total, int64_t plane, int nq, int64_t sz, int64_t sw,
+                                int paired) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t lat = i % plane;
+    int64_t r = i / plane;
+    if (!paired) {
+      const int64_t kq = r % nq, wi = r / nq;
+      const float* p = c + wi * sw + kq * sz + lat;
+      q[i] = make_float4(p[0], p[sz], p[2 * sz], p[3 * sz]);
+    } else {
+      const int64_t h = r % 2;
+      r /= 2;
+      const int64_t kq = r % nq, wi = r / nq;
+      const float* p = c + wi * sw + (kq + 2 * h) * sz + lat;
+      q[i] = make_float4(p[0], p[sw], p[sz], p[sz + sw]);
+    }
+  }
+}
+
+int64_t zq_entries(const ModelDev& m) {
+  const int64_t plane = (int64_t)m.cd[0] * m.cd[1], nq = m.n[2];
+  if (nq < 1) return 0;
+  switch (m.fittype) {
+    case kFit4Pi: return (int64_t)m.cd[3] * nq * plane;
+    case 7: return (int64_t)(m.cd[3] - 1) * nq * 2 * plane;
+    default: return 0;
+  }
+}
+
+void set_zq(ModelDev& m, float4* zq) {
+  const int64_t plane = (int64_t)m.cd[0] * m.cd[1], nq = m.n[2];
+  m.zq = zq;
+  m.zq_kz = m.zq_w = 0;
+  if (!zq) return;
+  if (m.fittype == 7) {
+    m.zq_kz = 2 * plane;
+    m.zq_w = 2 * nq * plane;
+  } else {
+    m.zq_kz = plane;
+    m.zq_w = nq * plane;
+  }
+}
+
+cudaError_t build_zq(const ModelDev& m, float4* zq, cudaStream_t stream) {
+  const int64_t total = zq_entries(m);
+  if (total <= 0) return cudaSuccess;
+  const int64_t blocks = (total + 255) / 256;
+  build_zq_kernel<<<(unsigned)(blocks < 8192 ? blocks : 8192), 256, 0, stream>>>(
+      m.coeff, zq, total, (int64_t)m.cd[0] * m.cd[1], m.n[2], m.st[2], m.st[3],
+      m.fittype == 7 ? 1 : 0);
+  return cudaGetLastError();
+}
+
 int warp_smem_floats(int mode, int s, bool var, int stg) {
   return make_layout(mode, s, var, stg).total();
 }

@@ -421,7 +421,8 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
     const int nodes = wx * wy;
     if constexpr (D == 3) {
       // one base pointer per z plane and 32-bit lateral offsets (lateral
-      // planes hold fewer than 2^29 elements)
+      // planes hold fewer than 2^29 elements); a 16-byte gather table as for
+      // the 4D models measured no faster here (its lower L1 hit rate)
       const float* b0 = m.coeff + (int64_t)(kz - 1) * sz_;
       const float* b1 = b0 + sz_;
       const float* b2 = b1 + sz_;
@@ -441,47 +442,41 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       const float* ww = w + 3 * 8;
       const float bw[4] = {ww[0], ww[1], ww[2], ww[3]};
       const float dw[3] = {ww[4], ww[5], ww[6]};
-      const int64_t sw_ = m.st[3];
-      // one base pointer per w layer and 32-bit offsets within it (the lateral
-      // node plus up to three z planes: lateral planes hold fewer than 2^29
-      // elements)
-      // (fit type 7; the 4Pi kernel keeps 64-bit addressing, which measured
-      // faster within its register budget)
-      const float* pw[4];
-      pw[0] = m.coeff + (int64_t)(kz - 1) * sz_ + (int64_t)(kw - 1) * sw_;
-#pragma unroll
-      for (int iw = 1; iw < 4; ++iw) pw[iw] = pw[iw - 1] + sw_;
-      const int st1 = (int)m.st[1], sz32 = (int)sz_;
+      // Gathers from the gather table: per node, 16-byte entries at 32-bit
+      // lateral offsets from one base per entry set (lateral planes hold fewer
+      // than 2^29 elements).
+      const int st1 = (int)m.st[1];
       Stride2D ix(lane, wy);
       const float2 BZ0 = bc2(bz0), BZ1 = bc2(bz1), BZ2 = bc2(bz2), BZ3 = bc2(bz3);
       const float2 DZ0 = bc2(dz0), DZ1 = bc2(dz1), DZ2 = bc2(dz2);
+      // 4Pi: the four z planes of layer kw - 1 + iw at q4 + iw * zq_w; fit
+      // type 7: layers (kw - 1, kw) at qp[0], (kw + 1, kw + 2) at qp[1], planes
+      // 0, 1 in the entry at the node's offset and 2, 3 one plane further.
+      const float4* q4 = m.zq + (int64_t)(kw - 1) * m.zq_w + (int64_t)(kz - 1) * m.zq_kz;
+      const float4* qp[2] = {q4, q4 + 2 * m.zq_w};
+      const int plane = (int)m.st[2];
       for (int t = lane; t < nodes; t += 32, ix.next()) {
         const int xr = ix.r, yr = ix.c;
         const int o0 = (xb + xr) * st1 + (yb + yr);
-        const int o1 = o0 + sz32, o2 = o1 + sz32, o3 = o2 + sz32;
         // z contraction of the four w layers: two layers per packed operation
         // (fit type 7), or one at a time where the packed operands would push
         // the kernel past its register budget (4Pi, four channels); both
         // orders of operations are the same.
         float vz[4], dzv[4];
         if constexpr (MODE == kFit4Pi) {
-          const float* p = pw[0] + (int64_t)(xb + xr) * m.st[1] + (yb + yr);
+          const float4* p = q4 + o0;
 #pragma unroll
           for (int iw = 0; iw < 4; ++iw) {
-            const float* q = p + iw * sw_;
-            const float c0 = __ldg(q), c1 = __ldg(q + sz_), c2 = __ldg(q + 2 * sz_), c3 = __ldg(q + 3 * sz_);
-            vz[iw] = contract4(c0, c1, c2, c3, bz0, bz1, bz2, bz3);
-            dzv[iw] = dcontract4(c0, c1, c2, c3, dz0, dz1, dz2);
+            const float4 cq = __ldg(p + iw * m.zq_w);
+            vz[iw] = contract4(cq.x, cq.y, cq.z, cq.w, bz0, bz1, bz2, bz3);
+            dzv[iw] = dcontract4(cq.x, cq.y, cq.z, cq.w, dz0, dz1, dz2);
           }
         } else {
 #pragma unroll
           for (int ip = 0; ip < 2; ++ip) {
-            const float* q0 = pw[2 * ip];
-            const float* q1 = pw[2 * ip + 1];
-            const float2 c0 = make_float2(__ldg(q0 + o0), __ldg(q1 + o0));
-            const float2 c1 = make_float2(__ldg(q0 + o1), __ldg(q1 + o1));
-            const float2 c2 = make_float2(__ldg(q0 + o2), __ldg(q1 + o2));
-            const float2 c3 = make_float2(__ldg(q0 + o3), __ldg(q1 + o3));
+            const float4 e01 = __ldg(qp[ip] + o0), e23 = __ldg(qp[ip] + plane + o0);
+            const float2 c0 = make_float2(e01.x, e01.y), c1 = make_float2(e01.z, e01.w);
+            const float2 c2 = make_float2(e23.x, e23.y), c3 = make_float2(e23.z, e23.w);
             const float2 v2 = contract4x2(c0, c1, c2, c3, BZ0, BZ1, BZ2, BZ3);
             const float2 d2 = dcontract4x2(c0, c1, c2, c3, DZ0, DZ1, DZ2);
             vz[2 * ip] = v2.x;

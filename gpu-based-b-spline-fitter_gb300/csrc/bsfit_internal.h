@@ -24,7 +24,23 @@ struct ModelDev {
   float init_p[4];
   int init_p_len;
   float shift[4];        // 4Pi models: per-channel phase shifts (knot units)
+  // Stage-A gather table of the FP32 kernels (build_zq), device; null for fit
+  // types 6 and 8. Per lateral node, the four z planes of one z knot as one
+  // 16-byte entry (4Pi: one per w layer), or for fit type 7 two adjacent w
+  // layers of them interleaved in two entries (planes 0, 1 and 2, 3 of both
+  // layers), so that a node's gathers are 16-byte loads. Entry strides, with
+  // the lateral node innermost as in the coefficient table: zq_kz between
+  // consecutive z knots, zq_w between consecutive (first) w layers.
+  const float4* zq;
+  int64_t zq_kz, zq_w;
 };
+
+// Number of float4 entries of a model's stage-A gather table (0: none), and
+// its construction from the model's device coefficients on a stream.
+int64_t zq_entries(const ModelDev& m);
+cudaError_t build_zq(const ModelDev& m, float4* zq, cudaStream_t stream);
+// Sets m.zq and its strides for a table at zq (null clears them).
+void set_zq(ModelDev& m, float4* zq);
 
 struct FitArgs {
   ModelDev m;

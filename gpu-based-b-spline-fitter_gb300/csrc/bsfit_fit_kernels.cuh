@@ -167,9 +167,12 @@ struct ModeTraits<8> {
 // lanes per column in each pass of the warp at the same offsets in every
 // column. A's column stride is padded to the next value congruent to s modulo
 // 32, which puts those 32 lanes on 32 consecutive banks. G stores the maps of
-// one (X node, pixel row) item together, GP floats per item with GP odd, so
-// the consecutive items of a pass (stage B writes, stage C reads) sit an odd
-// stride apart: 32 distinct banks.
+// one (X node, pixel row) item together, GP floats per item, written and read
+// as 16-byte vectors where the item has 3 or 4 maps (GP = 4: a quarter-warp's
+// eight consecutive items cover the 32 banks), as 8-byte pairs for the 5D
+// model's 10 maps (GP = 10: a half-warp's sixteen consecutive items sit 10
+// banks apart, 2 banks each, all distinct), and otherwise with GP odd (the
+// consecutive items of a pass an odd stride apart: 32 distinct banks).
 struct WarpLayout {
   int s, s2p, wp, na, ng, nch, nvar;  // nvar: sCMOS variance planes (0 or nch)
   bool alias;
@@ -178,10 +181,11 @@ struct WarpLayout {
     return x + ((s - x) % 32 + 32) % 32;
   }
   __host__ __device__ constexpr int as() const { return bank_pad(na * wp, s); }  // A column stride
-  // G item stride: odd (bank-conflict-free scalar accesses), or 4 for the 3D
-  // model's three maps, read and written as one 16-byte vector per item (a
-  // quarter-warp's eight consecutive items fill the 32 banks)
-  __host__ __device__ constexpr int gp() const { return ng == 3 ? 4 : (ng | 1); }
+  // G item stride (see above): 4 for three or four maps (16-byte vectors), 10
+  // for ten (8-byte pairs), else odd (scalar accesses)
+  __host__ __device__ constexpr int gp() const {
+    return (ng == 3 || ng == 4) ? 4 : ng == 10 ? 10 : (ng | 1);
+  }
   __host__ __device__ constexpr int gs() const { return s * gp(); }             // G column stride
   __host__ __device__ constexpr int off_kx() const { return (nch + nvar) * s2p; }
   __host__ __device__ constexpr int off_ky() const { return off_kx() + ((s + 3) & ~3); }
@@ -239,7 +243,8 @@ constexpr bool layouts_disjoint() {
         for (int c = 0; c < L.wp; ++c)
           if ((c + 1) * L.gs() > L.a_rel() + c * L.as()) return false;
         if (L.as() < L.na * L.wp || L.gp() < L.ng || (L.as() - s) % 32 != 0 ||
-            (L.gp() % 2 == 0 && L.gp() != 4) || L.total() % 4 != 0 || L.off_g() % 4 != 0)
+            (L.gp() % 2 == 0 && L.gp() != 4 && L.gp() != 10) || L.total() % 4 != 0 ||
+            L.off_g() % 4 != 0)
           return false;
       }
   return true;
@@ -786,9 +791,13 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         float* go = G + (xr * s + py) * GP;
         if constexpr (MODE == 6) {
           *reinterpret_cast<float4*>(go) = make_float4(gv[0], gv[1], gv[2], 0.0f);
+        } else if constexpr (NG == 4) {
+          *reinterpret_cast<float4*>(go) = make_float4(gv[0], gv[1], gv[2], gv[3]);
         } else {
+          static_assert(NG == 10, "5D items are stored as map pairs");
 #pragma unroll
-          for (int c = 0; c < NG; ++c) go[c] = gv[c];
+          for (int c = 0; c < NG; c += 2)
+            *reinterpret_cast<float2*>(go + c) = make_float2(gv[c], gv[c + 1]);
         }
       }
     }
@@ -821,46 +830,51 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         dudt[3] = 1.0f;
         dudt[4] = N * dc;
         model = bg + N * f;
-      } else {
-      float g0 = g[0], g1 = g[GS], g2 = g[2 * GS], g3 = g[3 * GS];
-      float f = g0 * bx0 + g1 * bx1 + g2 * bx2 + g3 * bx3;
-      float dX = (g1 - g0) * dx0 + (g2 - g1) * dx1 + (g3 - g2) * dx2;
-      const float* gy = g + 1;
-      float dY = gy[0] * bx0 + gy[GS] * bx1 + gy[2 * GS] * bx2 + gy[3 * GS] * bx3;
-      dudt[0] = -N * dX;
-      dudt[1] = -N * dY;
-      dudt[2] = f;
-      dudt[3] = 1.0f;
-      if constexpr (MODE != 8) {
-#pragma unroll
-        for (int c = 1; c < TR::NA; ++c) {
-          const float* gc = g + (c + 1);
-          float dc = gc[0] * bx0 + gc[GS] * bx1 + gc[2 * GS] * bx2 + gc[3 * GS] * bx3;
-          dudt[3 + c] = N * dc;
-        }
+      } else if constexpr (MODE != 8) {
+        // the item's four maps as one vector per X node (value, d/dY, d/dz,
+        // d/dw)
+        const float4* g4 = reinterpret_cast<const float4*>(g);
+        const float4 q0 = g4[0], q1 = g4[s], q2 = g4[2 * s], q3 = g4[3 * s];
+        float f = q0.x * bx0 + q1.x * bx1 + q2.x * bx2 + q3.x * bx3;
+        float dX = (q1.x - q0.x) * dx0 + (q2.x - q1.x) * dx1 + (q3.x - q2.x) * dx2;
+        float dY = q0.y * bx0 + q1.y * bx1 + q2.y * bx2 + q3.y * bx3;
+        float dz = q0.z * bx0 + q1.z * bx1 + q2.z * bx2 + q3.z * bx3;
+        float dw = q0.w * bx0 + q1.w * bx1 + q2.w * bx2 + q3.w * bx3;
+        dudt[0] = -N * dX;
+        dudt[1] = -N * dY;
+        dudt[2] = f;
+        dudt[3] = 1.0f;
+        dudt[4] = N * dz;
+        dudt[5] = N * dw;
         if (MODE == 7 && dup45) dudt[5] = dudt[4];
         model = bg + N * f;
       } else {
+        // 5D: the item's ten maps as five pairs per X node: (value, d/dY),
+        // (d/dz, d/dw), (d/du, z correction), (u correction, 3D value),
+        // (3D d/dY, 3D d/dz)
+        float2 q[4][5];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+          for (int c = 0; c < 5; ++c) q[k][c] = reinterpret_cast<const float2*>(g + k * GS)[c];
+        float f = q[0][0].x * bx0 + q[1][0].x * bx1 + q[2][0].x * bx2 + q[3][0].x * bx3;
+        float dX = (q[1][0].x - q[0][0].x) * dx0 + (q[2][0].x - q[1][0].x) * dx1 +
+                   (q[3][0].x - q[2][0].x) * dx2;
+        float dY = q[0][0].y * bx0 + q[1][0].y * bx1 + q[2][0].y * bx2 + q[3][0].y * bx3;
+        dudt[0] = -N * dX;
+        dudt[1] = -N * dY;
         // 5D derivatives with the reference's two term corrections
-        const float* gz = g + 2;
-        const float* gw = g + 3;
-        const float* gu = g + 4;
-        const float* gqz = g + 5;
-        const float* gqu = g + 6;
-        float dZ = gz[0] * bx0 + gz[GS] * bx1 + gz[2 * GS] * bx2 + gz[3 * GS] * bx3 +
-                   (gqz[2 * GS] * bx2 + gqz[3 * GS] * bx3);
-        float dW = gw[0] * bx0 + gw[GS] * bx1 + gw[2 * GS] * bx2 + gw[3 * GS] * bx3;
-        float dU = gu[0] * bx0 + gu[GS] * bx1 + gu[2 * GS] * bx2 + gu[3 * GS] * bx3 +
-                   (gqu[0] * bx0 + gqu[GS] * bx1);
+        float dZ = q[0][1].x * bx0 + q[1][1].x * bx1 + q[2][1].x * bx2 + q[3][1].x * bx3 +
+                   (q[2][2].y * bx2 + q[3][2].y * bx3);
+        float dW = q[0][1].y * bx0 + q[1][1].y * bx1 + q[2][1].y * bx2 + q[3][1].y * bx3;
+        float dU = q[0][2].x * bx0 + q[1][2].x * bx1 + q[2][2].x * bx2 + q[3][2].x * bx3 +
+                   (q[0][3].x * bx0 + q[1][3].x * bx1);
         // 3D spline
-        const float* h = g + 7;
-        float h0 = h[0], h1 = h[GS], h2 = h[2 * GS], h3 = h[3 * GS];
+        float h0 = q[0][3].y, h1 = q[1][3].y, h2 = q[2][3].y, h3 = q[3][3].y;
         float f3 = h0 * bx0 + h1 * bx1 + h2 * bx2 + h3 * bx3;
         float dX3 = (h1 - h0) * dx0 + (h2 - h1) * dx1 + (h3 - h2) * dx2;
-        const float* hy = g + 8;
-        float dY3 = hy[0] * bx0 + hy[GS] * bx1 + hy[2 * GS] * bx2 + hy[3 * GS] * bx3;
-        const float* hz = g + 9;
-        float dZ3 = hz[0] * bx0 + hz[GS] * bx1 + hz[2 * GS] * bx2 + hz[3 * GS] * bx3;
+        float dY3 = q[0][4].x * bx0 + q[1][4].x * bx1 + q[2][4].x * bx2 + q[3][4].x * bx3;
+        float dZ3 = q[0][4].y * bx0 + q[1][4].y * bx1 + q[2][4].y * bx2 + q[3][4].y * bx3;
         // mixture (CPUmleFit_LM.cpp:3311-3322)
         const float g2 = th[7], h2m = 1.0f - g2;
         const float m5 = bg + N * f, m3 = bg + N * f3;
@@ -874,7 +888,6 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         // m5 - m3 = N (f5 - f3): formed without the background, which cancels
         dudt[NV - 1] = N * (f - f3);
         model = m3 * h2m + m5 * g2;
-      }
       }
       float d = data[p];
       if constexpr (VAR) {

@@ -24,7 +24,7 @@ struct bsfit_model_s {
   ModelDev dev;
   float* d_coeff = nullptr;
   float* d_coeff3 = nullptr;
-  float4* d_zq = nullptr;  // stage-A gather table of the FP32 kernels (fit type 7, 4Pi)
+  float4* d_zq = nullptr;  // stage-A gather table of the FP32 kernels (fit types 7, 8, 4Pi)
   // Double copies for the FP64 reference-precision fit, made on first use.
   double* d_coeff64 = nullptr;
   double* d_coeff3_64 = nullptr;

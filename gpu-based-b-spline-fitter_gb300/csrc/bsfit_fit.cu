@@ -14,14 +14,15 @@ namespace bsfit {
 // k - 1 .. k + 2):
 //   4Pi: i = (wi * nq + kq) * P + lat holds planes kq .. kq + 3 of w layer wi
 //     at lateral node lat;
+//   fit type 8: i = kq * P + lat, the same for the 3D table of the mixture;
 //   fit type 7: i = ((wi * nq + kq) * 2 + h) * P + lat holds planes kq + 2h and
 //     kq + 2h + 1 of layers wi and wi + 1, as (plane 0 layer wi, plane 0 layer
 //     wi + 1, plane 1 layer wi, plane 1 layer wi + 1), for first layers
 //     wi = 0 .. nW - 2 (the kernel pairs w layers kw - 1, kw and kw + 1, kw + 2).
 // Every read stays inside the table: kq + 3 <= n[2] + 2 = nZ - 1, wi + 1 <= nW - 1.
 // The 3D kernels read the coefficient table itself (a table of this kind
-// measured no faster there) and the 5D one would not stay L2-resident at 4x
-// its 56 MB.
+// measured no faster there), and so does the 5D part of fit type 8 (at 4x its
+// 56 MB it would not stay L2-resident).
 
 __global__ void build_zq_kernel(const float* __restrict__ c, float4* __restrict__ q,
                                 int64_t total, int64_t plane, int nq, int64_t sz, int64_t sw,
@@ -49,6 +50,7 @@ int64_t zq_entries(const ModelDev& m) {
   if (nq < 1) return 0;
   switch (m.fittype) {
     case kFit4Pi: return (int64_t)m.cd[3] * nq * plane;
+    case 8: return nq * plane;
     case 7: return (int64_t)(m.cd[3] - 1) * nq * 2 * plane;
     default: return 0;
   }
@@ -73,8 +75,8 @@ cudaError_t build_zq(const ModelDev& m, float4* zq, cudaStream_t stream) {
   if (total <= 0) return cudaSuccess;
   const int64_t blocks = (total + 255) / 256;
   build_zq_kernel<<<(unsigned)(blocks < 8192 ? blocks : 8192), 256, 0, stream>>>(
-      m.coeff, zq, total, (int64_t)m.cd[0] * m.cd[1], m.n[2], m.st[2], m.st[3],
-      m.fittype == 7 ? 1 : 0);
+      m.fittype == 8 ? m.coeff3 : m.coeff, zq, total, (int64_t)m.cd[0] * m.cd[1], m.n[2],
+      m.st[2], m.st[3], m.fittype == 7 ? 1 : 0);
   return cudaGetLastError();
 }
 

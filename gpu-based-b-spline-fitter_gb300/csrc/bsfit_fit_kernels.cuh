@@ -659,11 +659,17 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
       }
       cp_async_wait_all();
       } else {
+      // the 5D block by 64-bit node pointer and layer strides (uniform base
+      // pointers per (u, w) layer with 32-bit offsets, as the 3D and 4D stage A
+      // do, measured 3% slower here: they push the kernel into spills); the 3D
+      // part's four z planes from the gather table (32-bit lateral offsets)
+      const int st1 = (int)m.st[1];
+      const float4* q3 = m.zq + (int64_t)(kz - 1) * m.zq_kz;
       Stride2D ix(lane, wy);
       for (int t = lane; t < nodes; t += 32, ix.next()) {
         const int xr = ix.r, yr = ix.c;
-        const int64_t lat = (int64_t)(xb + xr) * m.st[1] + (yb + yr);
-        const float* p = base + lat;
+        const int o0 = (xb + xr) * st1 + (yb + yr);
+        const float* p = base + o0;
         // z contraction of the 16 (u, w) columns, u = 2k and 2k + 1 side by
         // side in one packed operation.
         float2 vz2[2][4], dzz2[2][4];  // [u pair][w]
@@ -722,8 +728,8 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const WarpLayout&
         for (int iw = 0; iw < 2; ++iw)
           qu += bw[iw] * ((sq[2][iw] - sq[1][iw]) - (sq[3][iw] - sq[2][iw]));
         qu *= du[2];
-        const float* p3 = base3 + lat;
-        float e0 = __ldg(p3), e1 = __ldg(p3 + sz_), e2 = __ldg(p3 + 2 * sz_), e3 = __ldg(p3 + 3 * sz_);
+        const float4 e = __ldg(q3 + o0);
+        const float e0 = e.x, e1 = e.y, e2 = e.z, e3 = e.w;
         float* o = A + xr * AS + yr;
         o[0] = v;
         o[wp] = dzv;

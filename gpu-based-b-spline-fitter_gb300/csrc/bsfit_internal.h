@@ -25,8 +25,9 @@ struct ModelDev {
   int init_p_len;
   float shift[4];        // 4Pi models: per-channel phase shifts (knot units)
   // Stage-A gather table of the FP32 kernels (build_zq), device; null for fit
-  // types 6 and 8. Per lateral node, the four z planes of one z knot as one
-  // 16-byte entry (4Pi: one per w layer), or for fit type 7 two adjacent w
+  // type 6. Per lateral node, the four z planes of one z knot as one 16-byte
+  // entry (4Pi: one per w layer; fit type 8: of its 3D table), or for fit
+  // type 7 two adjacent w
   // layers of them interleaved in two entries (planes 0, 1 and 2, 3 of both
   // layers), so that a node's gathers are 16-byte loads. Entry strides, with
   // the lateral node innermost as in the coefficient table: zq_kz between

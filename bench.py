@@ -675,6 +675,7 @@ def bench_gpu(args):
         if g.roi_size == 13:
             fits_3d13 = len(g.rois) / (t * 1e-3)
     fits_5d17 = None
+    tuned_models = {}
     if not args.no_5d:
         from bsfit import workloads as W
         w5 = W.workload_5d(args.rois_5d, s=17, stream=7)
@@ -682,6 +683,12 @@ def bench_gpu(args):
         r5 = torch.from_numpy(w5.rois).to(dev)
         o5 = (torch.empty((9, len(w5.rois)), device=dev), torch.empty((8, len(w5.rois)), device=dev),
               torch.empty((len(w5.rois),), device=dev))
+        if not args.no_tune:
+            # the tuner's choice for this model and size, on a sample of it
+            from bsfit import tuning as T
+            ch = T.autotune(m5, r5[:5000], w5.iterations, reps=2)
+            tuned_models["5d_17"] = {k: ch[k] for k in ("variant", "warps_per_block",
+                                                       "min_blocks", "ms")}
         with torch.cuda.stream(stream):
             m5.fit_torch(r5, w5.iterations, out=o5, stream=stream)
             a5, b5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -699,6 +706,11 @@ def bench_gpu(args):
         w7 = W.workload_4d(args.rois_4d, sizes=(13,), stream=6)[0]
         m7 = bsfit.Model(7, w7.coeff, init_p=w7.init_p)
         r7 = torch.from_numpy(w7.rois).to(dev)
+        if not args.no_tune:
+            from bsfit import tuning as T
+            ch = T.autotune(m7, r7[:20000], w7.iterations, reps=2)
+            tuned_models["4d_13"] = {k: ch[k] for k in ("variant", "warps_per_block",
+                                                       "min_blocks", "ms")}
         with torch.cuda.stream(stream):
             m7.fit_torch(r7, w7.iterations, stream=stream)
             a7, b7 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -905,7 +917,10 @@ def bench_gpu(args):
                        "4pi_workload": f"{args.rois_4pi} ROIs of 4 channels 13x13, 100 iterations"},
         "autotune": {"per_size": tuned,
                      "sample": f"{args.tune_rois} ROIs of each size group",
-                     "batched_uses": str(max(SIZES))} if tuned else None,
+                     "batched_uses": str(max(SIZES)),
+                     "per_model": tuned_models,
+                     "per_model_sample": "20000 ROIs of the 4D figure, 5000 of the 5D figure"}
+        if tuned else None,
         "config_3_colour": c3_fig,
         "config_4_4pi": c4_fig,
         "parity_precision": parity_fig,

@@ -112,7 +112,11 @@ int bsfit_measure_fp32_peaks(double* scalar_tflops, double* paired_tflops);
 /*
  * Device-resident model: the coefficient tables of one PSF model uploaded once
  * and reused across calls (the reference uploads them on every call,
- * mex :484-518). Copies from host memory; coeff3 only for fit type 8.
+ * mex :484-518). Copies from host memory; coeff3 only for fit type 8. Beside
+ * the tables the model holds a gather table for the FP32 kernels (the z planes
+ * of each lateral node packed in 16-byte entries): 8x the coefficient table for
+ * fit type 7, 4x for 4Pi, 4x coeff3 for fit type 8, none for fit type 6. The
+ * call returns after the tables are built.
  */
 typedef struct bsfit_model_s* bsfit_model;
 

@@ -411,7 +411,8 @@ template <int MODE>
 __device__ __forceinline__ void channel_pass(const FitArgs& a, const Layout& L, float* ws, int lane,
                                              const dd* th, bool dup45, bool fisher, Acc& err,
                                              Acc (&acc)[Traits<MODE>::NV + Traits<MODE>::NV *
-                                                                                (Traits<MODE>::NV + 1) / 2]) {
+                                                                                (Traits<MODE>::NV + 1) / 2],
+                                             bool maps_ready = false) {
   using TR = Traits<MODE>;
   constexpr int D = TR::D;
   constexpr int NV = TR::NV;
@@ -472,8 +473,10 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const Layout& L, 
     return dd{v.x, v.y};
   };
 
-  // (A) non-lateral contraction at every lateral node of the window
-  {
+  // (A) non-lateral contraction at every lateral node of the window; skipped
+  // with maps_ready (the workspace holds the maps of the previous evaluation,
+  // made at the same spatial parameters)
+  if (!maps_ready) {
     dd bz[4], dz[3];
 #pragma unroll
     for (int q = 0; q < 4; ++q) bz[q] = W(2, q);
@@ -667,7 +670,7 @@ __device__ __forceinline__ void channel_pass(const FitArgs& a, const Layout& L, 
   __syncwarp();
 
   // (B) Y contraction for every (X node, pixel row)
-  {
+  if (!maps_ready) {
     dd by[4], dy[3];
 #pragma unroll
     for (int q = 0; q < 4; ++q) by[q] = W(0, q);
@@ -905,7 +908,8 @@ __device__ __forceinline__ dd warp_sum_dd(dd v) {
 // Fisher) row l (hr); the deviance (or log-likelihood) is on every lane.
 template <int MODE>
 __device__ void evaluate(const FitArgs& a, const Layout& L, float* ws, int lane, const dd* th,
-                         bool dup45, bool fisher, dd& err_out, dd& gl, dd (&hr)[Traits<MODE>::NV]) {
+                         bool dup45, bool fisher, dd& err_out, dd& gl, dd (&hr)[Traits<MODE>::NV],
+                         bool maps_ready = false) {
   constexpr int NV = Traits<MODE>::NV;
   constexpr int K = NV + NV * (NV + 1) / 2;
   Acc err;
@@ -913,7 +917,7 @@ __device__ void evaluate(const FitArgs& a, const Layout& L, float* ws, int lane,
   Acc acc[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k].zero();
-  channel_pass<MODE>(a, L, ws, lane, th, dup45, fisher, err, acc);
+  channel_pass<MODE>(a, L, ws, lane, th, dup45, fisher, err, acc, maps_ready);
   dd v[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) v[k] = acc[k].get();
@@ -1090,8 +1094,20 @@ __device__ Result fit_roi(const FitArgs& a, const Layout& L, float* ws, int lane
     }
   }
   dd ll = mk(0.0f);
+  bool evaluated = false;  // the workspace holds maps of this ROI's last evaluation
   for (;;) {
     if (need_eval) {
+      // The CRLB pass at the position of this kernel's last evaluation reuses
+      // its stage-A/B maps (they depend on the spatial parameters only). Not
+      // for fit type 8, whose kernel the extra state pushes into more spills
+      // (measured 3% slower).
+      bool maps_ready = false;
+      if (MODE != 8 && fisher && evaluated) {
+        const bool spatial = lane < NV && lane != 2 && lane != 3;
+        const bool same = !spatial || (__float_as_uint(par.hi) == __float_as_uint(par_eval.hi) &&
+                                       __float_as_uint(par.lo) == __float_as_uint(par_eval.lo));
+        maps_ready = __all_sync(kFull, same);
+      }
       if (!fisher) par_eval = par;
       dd the[NV];
       // (a hand-off may enter here with fisher set: par_eval is then the
@@ -1100,9 +1116,10 @@ __device__ Result fit_roi(const FitArgs& a, const Layout& L, float* ws, int lane
       for (int k = 0; k < NV; ++k)
         the[k] = shfl((MODE == 8 && fisher && k != 2 && k != 3) ? par_eval : par, k);
       dd e;
-      evaluate<MODE>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr);
+      evaluate<MODE>(a, L, ws, lane, the, first && MODE == 7, fisher, e, gl, hr, maps_ready);
       first = false;
       need_eval = false;
+      evaluated = true;
       if (fisher) {
         ll = e;
         break;

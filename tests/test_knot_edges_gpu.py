@@ -65,7 +65,12 @@ def test_eval_at_knot_range_edges(bsfit_mod, oracle, case):
                           coeff3=c3)
         assert np.isfinite(g).all() and np.isfinite(ref).all()
         diag = np.stack([ref[:, 1 + nv + idx.index((k, k))] for k in range(nv)], 1)
-        diag = np.maximum(diag, 1e-6 * np.median(diag, 0))
+        # At these edges some derivatives vanish identically (the curvature of
+        # z, w or u drops to 1e-13..1e-33 on the mirror-padded boundary knots),
+        # where the FP32 sums keep rounding noise of the terms' usual size: the
+        # curvature floor is 1e-3 of the parameter's median curvature (1e-6 at
+        # the interior positions of the fixed-parameter test).
+        diag = np.maximum(diag, 1e-3 * np.median(diag, 0))
         e0 = np.abs(g[:, 0] - ref[:, 0]).max() / np.abs(ref[:, 0]).max()
         eJ = (np.abs(g[:, 1:1 + nv] - ref[:, 1:1 + nv]) / np.sqrt(diag)).max()
         eH = max((np.abs(g[:, 1 + nv + i] - ref[:, 1 + nv + i]) /

@@ -175,8 +175,7 @@ cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t 
     kern = batch_variant(mode, tc.variant);
   if (!kern) return cudaErrorInvalidValue;
   const int rpw = tune_rois_per_warp(mode, tc.variant);
-  const int per_warp =
-      rpw * warp_smem_floats(mode, a.s_max, false, tune_staged(mode, tc.variant)) * 4;
+  const int per_warp = tune_warp_floats(mode, tc.variant, a.s_max, false) * 4;
   int wpb = 4, blocks_per_sm = 0, sms = 0;
   cudaError_t e = pick_launch_wpb((const void*)kern, per_warp, multi ? 0 : tc.wpb, &wpb,
                                   &blocks_per_sm, &sms);
@@ -377,10 +376,10 @@ cudaError_t launch_fit(const FitArgs& a, cudaStream_t stream) {
       tc.variant > 0)
     kern = fit_variant(mode, tc.variant);
   if (!kern) return cudaErrorInvalidValue;
-  // ROIs per warp: 2 for the pair variants of fit type 6 (two workspaces per warp)
+  // ROIs per warp: 2 for the pair and packed variants of fit type 6
   const int rpw = tunable ? tune_rois_per_warp(mode, tc.variant) : 1;
   const int per_warp =
-      rpw * warp_smem_floats(mode, a.s, var, tunable ? tune_staged(mode, tc.variant) : 0) * 4;
+      (tunable ? tune_warp_floats(mode, tc.variant, a.s, var) : warp_smem_floats(mode, a.s, var)) * 4;
   int wpb = 4, blocks_per_sm = 0, sms = 0;
   cudaError_t e = pick_launch_wpb((const void*)kern, per_warp, tunable ? tc.wpb : 0, &wpb,
                                   &blocks_per_sm, &sms);

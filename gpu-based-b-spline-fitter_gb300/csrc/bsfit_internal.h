@@ -203,8 +203,10 @@ int tune_min_blocks(int mode, int variant);
 // 1 when the variant stages the 5D gathers through shared memory (its
 // per-warp shared memory includes the staging buffers)
 int tune_staged(int mode, int variant);
-// ROIs fitted per warp by a variant (2: the half-warp pair form of fit type 6)
+// ROIs fitted per warp by a variant (2: the pair and packed forms of fit type 6)
 int tune_rois_per_warp(int mode, int variant);
+// Shared-memory floats per warp of a variant at ROI size s
+int tune_warp_floats(int mode, int variant, int s, bool var);
 FitKern fit_variant(int mode, int variant);     // variant >= 1
 BatchKern batch_variant(int mode, int variant);  // variant >= 1
 bool tune_lookup(int mode, int s, int dev, TuneConfig* out);

@@ -243,17 +243,23 @@ struct PairClaim {
   }
 };
 
-// Fit every ROI the two halves claim, until both find none left. done:
-// optional counter of finished ROIs (the batched form's).
-__device__ __forceinline__ void fit_pair(const FitArgs& a, const WarpLayout& L, float* ws,
-                                         int lane, PairClaim& claim, unsigned long long* done_ctr) {
+// Fit every ROI the two halves claim, until both find none left. Each half
+// stages its ROI's pixels at pix (its own) and keeps its LM state on its 16
+// lanes; eval(par, fisher, err, gl, hr) evaluates both halves' ROIs at once
+// (lane l of a half holds its ROI's parameter l and mode) and returns each
+// half's deviance (or log-likelihood), gradient entry and Hessian (or Fisher)
+// row on its lanes, as evaluate() does for one ROI. done: optional counter of
+// finished ROIs (the batched form's).
+template <class Eval>
+__device__ __forceinline__ void fit_pair_loop(const FitArgs& a, int s, float* pix, int lane,
+                                              PairClaim& claim, unsigned long long* done_ctr,
+                                              Eval&& eval) {
   constexpr int MODE = 6;
   constexpr int NV = 5;
   constexpr int kNew = 0, kRun = 1, kOut = 2;
   const int hl = lane & 15;
   const int hb = lane & 16;
   const unsigned hm = hb ? 0xffff0000u : 0x0000ffffu;
-  const int s = L.s;
   const int s2 = s * s;
 
   int st = kNew;
@@ -283,11 +289,11 @@ __device__ __forceinline__ void fit_pair(const FitArgs& a, const WarpLayout& L, 
       }
       if (ld) {
         const float* src = a.rois + roi * (int64_t)s2;
-        for (int p = hl; p < s2; p += 16) ws[p] = __ldg(src + p);
+        for (int p = hl; p < s2; p += 16) pix[p] = __ldg(src + p);
       }
       __syncwarp();
       float g[4];
-      initial_guess_pair(ws, s, hl, hm, g);
+      initial_guess_pair(pix, s, hl, hm, g);
       if (ld) {
         // CPUmleFit_LM.cpp:2425-2450, 2477-2482: lane l keeps parameter l
         float v = 0.0f;
@@ -316,12 +322,9 @@ __device__ __forceinline__ void fit_pair(const FitArgs& a, const WarpLayout& L, 
     // (2) one evaluation of both halves; a half that needs none (a failed
     // solve, or no ROI) ignores its result
     {
-      float the[NV];
-#pragma unroll
-      for (int k = 0; k < NV; ++k) the[k] = hbcast(par, hb, k);
       FPair e;
       float gn, hn[NV];
-      evaluate_pair(a, L, ws, hl, hb, hm, the, fisher, e, gn, hn);
+      eval(par, fisher, e, gn, hn);
       if (st == kRun && need_eval) {
         gl = gn;
 #pragma unroll
@@ -535,6 +538,22 @@ __device__ __forceinline__ void fit_pair(const FitArgs& a, const WarpLayout& L, 
       }
     }
   }
+}
+
+// The half-warp pair form: each half evaluates its own ROI in its own
+// workspace with 16 lanes (evaluate_pair).
+__device__ __forceinline__ void fit_pair(const FitArgs& a, const WarpLayout& L, float* ws,
+                                         int lane, PairClaim& claim, unsigned long long* done_ctr) {
+  const int hl = lane & 15;
+  const int hb = lane & 16;
+  const unsigned hm = hb ? 0xffff0000u : 0x0000ffffu;
+  fit_pair_loop(a, L.s, ws, lane, claim, done_ctr,
+                [&](float par, bool fisher, FPair& e, float& gn, float (&hn)[5]) {
+                  float the[5];
+#pragma unroll
+                  for (int k = 0; k < 5; ++k) the[k] = hbcast(par, hb, k);
+                  evaluate_pair(a, L, ws, hl, hb, hm, the, fisher, e, gn, hn);
+                });
 }
 
 // Plain form: FitArgs as fit_kernel<6>; each warp holds two workspaces.

@@ -12,9 +12,11 @@
 //    the SM's shared memory;
 //  - for fit type 8, the staging of stage A's gathers: into registers, or into
 //    shared memory with asynchronous copies one round of 32 nodes ahead;
-//  - for fit type 6, the ROIs per warp: one (32 lanes per ROI), or two (one per
-//    half-warp, bsfit_pair.cuh), which shares the per-evaluation work that does
-//    not grow with the ROI between two ROIs at twice the shared memory per warp.
+//  - for fit type 6, the ROIs per warp: one (32 lanes per ROI), or two, either
+//    one per half-warp (bsfit_pair.cuh), which shares the per-evaluation work
+//    that does not grow with the ROI between two ROIs at twice the shared
+//    memory per warp, or both on all 32 lanes in the two halves of paired FP32
+//    operations (bsfit_pack.cuh), which shares the whole evaluation.
 // Variant 0 is the default kernel (bsfit_fit.cu); this file instantiates the
 // others. Every variant runs the same code, so results are bit-identical
 // across configurations. A table per (fit type, ROI size, device) holds the
@@ -22,15 +24,19 @@
 #include <mutex>
 
 #include "bsfit_fit_kernels.cuh"
+#include "bsfit_pack.cuh"
 #include "bsfit_pair.cuh"
 
 namespace bsfit {
 
 namespace {
 
-// fit type 6: variants 3 to 5 fit two ROIs per warp
-constexpr int kMinBlocks6[6] = {BSFIT_MINBLOCKS(6), 5, 4, 6, 5, 4};
-constexpr int kRoisPerWarp6[6] = {1, 1, 1, 2, 2, 2};
+// fit type 6: variants 3 to 5 fit two ROIs per warp on its halves, 6 and 7
+// two ROIs per warp in paired operations
+constexpr int kNumVariants6 = 8;
+constexpr int kMinBlocks6[kNumVariants6] = {BSFIT_MINBLOCKS(6), 5, 4, 6, 5, 4, 4, 3};
+constexpr int kRoisPerWarp6[kNumVariants6] = {1, 1, 1, 2, 2, 2, 2, 2};
+constexpr bool kPacked6[kNumVariants6] = {false, false, false, false, false, false, true, true};
 constexpr int kMinBlocks7[3] = {BSFIT_MINBLOCKS(7), 3, 5};
 // fit type 8: variants 2 and 3 stage the 5D gathers through shared memory
 // (cp.async, two rounds of 32 nodes in flight per warp)
@@ -48,10 +54,18 @@ int g_ntune = 0;
 
 }  // namespace
 
-int tune_num_variants(int mode) { return mode == 6 ? 6 : mode == 7 ? 3 : mode == 8 ? 4 : 0; }
+int tune_num_variants(int mode) {
+  return mode == 6 ? kNumVariants6 : mode == 7 ? 3 : mode == 8 ? 4 : 0;
+}
 
 int tune_rois_per_warp(int mode, int variant) {
-  return (mode == 6 && variant >= 0 && variant < 6) ? kRoisPerWarp6[variant] : 1;
+  return (mode == 6 && variant >= 0 && variant < kNumVariants6) ? kRoisPerWarp6[variant] : 1;
+}
+
+int tune_warp_floats(int mode, int variant, int s, bool var) {
+  if (mode == 6 && variant >= 0 && variant < kNumVariants6 && kPacked6[variant])
+    return make_pack_layout(s).total();
+  return tune_rois_per_warp(mode, variant) * warp_smem_floats(mode, s, var, tune_staged(mode, variant));
 }
 
 int tune_staged(int mode, int variant) {
@@ -70,6 +84,8 @@ FitKern fit_variant(int mode, int variant) {
     case 63: return fit_pair_kernel<kMinBlocks6[3]>;
     case 64: return fit_pair_kernel<kMinBlocks6[4]>;
     case 65: return fit_pair_kernel<kMinBlocks6[5]>;
+    case 66: return fit_pack_kernel<kMinBlocks6[6]>;
+    case 67: return fit_pack_kernel<kMinBlocks6[7]>;
     case 71: return fit_kernel<7, false, false, kMinBlocks7[1]>;
     case 72: return fit_kernel<7, false, false, kMinBlocks7[2]>;
     case 81: return fit_kernel<8, false, false, kMinBlocks8[1]>;
@@ -86,6 +102,8 @@ BatchKern batch_variant(int mode, int variant) {
     case 63: return batch_pair_kernel<kMinBlocks6[3]>;
     case 64: return batch_pair_kernel<kMinBlocks6[4]>;
     case 65: return batch_pair_kernel<kMinBlocks6[5]>;
+    case 66: return batch_pack_kernel<kMinBlocks6[6]>;
+    case 67: return batch_pack_kernel<kMinBlocks6[7]>;
     case 71: return batch_kernel<7, false, kMinBlocks7[1]>;
     case 72: return batch_kernel<7, false, kMinBlocks7[2]>;
     case 81: return batch_kernel<8, false, kMinBlocks8[1]>;

@@ -1,8 +1,10 @@
-"""The two-ROIs-per-warp form of the 3D kernels (fit type 6, tuner variants 3 to
-5) gives the one-ROI form's outputs bit for bit at every ROI size: small and
-large ROIs (one or two pixel chains per lane, windows of one or two rounds),
-ROIs with NaN, zero and negative pixels, iteration caps of 0 and 1, an odd ROI
-count (one half of a warp without a ROI), plain and batched with several sizes."""
+"""The two-ROIs-per-warp forms of the 3D kernels (fit type 6: tuner variants 3
+to 5, one ROI per half-warp; 6 and 7, both ROIs on all lanes in paired
+operations) give the one-ROI form's outputs bit for bit at every ROI size:
+small and large ROIs (one or two pixel chains per lane, windows of one or two
+rounds), ROIs with NaN, zero and negative pixels (whose windows differ from the
+other slot's), iteration caps of 0 and 1, an odd ROI count (one half of a warp
+without a ROI), plain and batched with several sizes."""
 import numpy as np
 import pytest
 
@@ -10,7 +12,7 @@ from test_fit_gpu import bsfit_mod  # noqa: F401
 
 pytestmark = pytest.mark.gpu
 
-PAIR_VARIANTS = (3, 5)
+PAIR_VARIANTS = (3, 5, 6, 7)
 
 
 def _rois(s, n, stream):

@@ -56,12 +56,13 @@ def test_variant_table():
     """Variant 0 is each fit type's default register budget (6 resident
     4-warp blocks for 3D, 4 for 4D, 3 for 5D); the others are alternatives
     (fit type 8's variants 2 and 3 stage the 5D gathers through shared memory;
-    fit type 6's variants 3 to 5 fit two ROIs per warp)."""
+    fit type 6's variants 3 to 7 fit two ROIs per warp: 3 to 5 one per
+    half-warp, 6 and 7 both in paired operations on all lanes)."""
     from bsfit import tuning as T
-    assert [T.num_variants(f) for f in (5, 6, 7, 8)] == [0, 6, 3, 4]
-    assert [T.min_blocks(6, v) for v in range(6)] == [6, 5, 4, 6, 5, 4]
-    assert [T.rois_per_warp(6, v) for v in range(6)] == [1, 1, 1, 2, 2, 2]
-    assert [T.rois_per_warp(f, 0) for f in (7, 8)] == [1, 1] and T.rois_per_warp(6, 6) == 0
+    assert [T.num_variants(f) for f in (5, 6, 7, 8)] == [0, 8, 3, 4]
+    assert [T.min_blocks(6, v) for v in range(8)] == [6, 5, 4, 6, 5, 4, 4, 3]
+    assert [T.rois_per_warp(6, v) for v in range(8)] == [1, 1, 1, 2, 2, 2, 2, 2]
+    assert [T.rois_per_warp(f, 0) for f in (7, 8)] == [1, 1] and T.rois_per_warp(6, 8) == 0
     assert [T.min_blocks(7, v) for v in range(3)] == [4, 3, 5]
     assert [T.min_blocks(8, v) for v in range(4)] == [3, 2, 2, 1]
     assert T.min_blocks(8, 4) == 0 and T.min_blocks(6, -1) == 0

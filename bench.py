@@ -458,6 +458,13 @@ def bench_serving(args, dev, seed=11):
     merged = {"merge": 4, "fits_per_s": n_rois / msat_s,
               "frame10k_mixed": mixed10k(srv, fm_sat_s)[1]}
     srv.close()
+    # priority launches: short requests on high-priority streams, long launches
+    # whose blocks retire as they finish (the same arrivals as above)
+    srv = bsfit.Server(max_inflight=4, arena_bytes=4 << 30, priority=True)
+    run_stream(srv, frames[:4], [0] * 4)  # warm-up
+    psat_s, _ = run_stream(srv, frames, [0] * len(frames))
+    prio = {"fits_per_s": n_rois / psat_s, "frame10k_mixed": mixed10k(srv, fm_sat_s)[1]}
+    srv.close()
     # plain per-call form
     t0 = time.perf_counter()
     for kind, w, r in frames:
@@ -476,7 +483,7 @@ def bench_serving(args, dev, seed=11):
             "loaded_fits_per_s": n_rois / load_s,
             "frame10k_3d": {"p50_ms": l10["p50_ms"], "p99_ms": l10["p99_ms"], "load": 0.7,
                             "saturated_p50_ms": s10["p50_ms"]},
-            "frame10k_mixed": mixed, "merged": merged,
+            "frame10k_mixed": mixed, "merged": merged, "priority": prio,
             "max_inflight": 4, "arena_bytes": 4 << 30}
 
 

@@ -481,17 +481,22 @@ class Server:
     the last call (P (N, NV+1), CRLB (N, NV), LL (N,) per segment, as
     GPUmleFit_LM_multiD); wait(id) blocks until one request is done."""
 
-    def __init__(self, max_inflight=4, arena_bytes=2 << 30, merge=1):
-        """merge: most queued requests fitted by one launch (bsfit_server_set_merge)."""
+    def __init__(self, max_inflight=4, arena_bytes=2 << 30, merge=1, priority=False):
+        """merge: most queued requests fitted by one launch (bsfit_server_set_merge);
+        priority: launches on streams of three priorities by their estimated
+        device time, with blocks that retire while they run
+        (bsfit_server_set_priority)."""
         h = np.ctypeslib.ctypes.c_void_p()
         check(_native.lib().bsfit_server_create(int(max_inflight), int(arena_bytes),
                                                 np.ctypeslib.ctypes.byref(h)), "bsfit_server_create")
         self._h = h
-        if merge != 1:
-            st = _native.lib().bsfit_server_set_merge(h, int(merge))
-            if st != 0:
-                self.close()
-                check(st, "bsfit_server_set_merge")
+        for on, fn, arg in ((merge != 1, "bsfit_server_set_merge", int(merge)),
+                            (bool(priority), "bsfit_server_set_priority", 1)):
+            if on:
+                st = getattr(_native.lib(), fn)(h, arg)
+                if st != 0:
+                    self.close()
+                    check(st, fn)
         self._live = {}
         self._done = {}  # results collected by poll() and not yet taken by wait()
 

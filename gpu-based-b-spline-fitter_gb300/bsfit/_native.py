@@ -77,6 +77,7 @@ SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_void_p)]),
     "bsfit_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "bsfit_server_set_merge": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "bsfit_server_set_priority": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "bsfit_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                            ctypes.POINTER(ctypes.c_int64)]),
     "bsfit_server_submit_multistart": (ctypes.c_int, [

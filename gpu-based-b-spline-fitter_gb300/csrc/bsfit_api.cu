@@ -383,9 +383,11 @@ int64_t bsfit_batch_scratch_bytes(int32_t nseg) {
 namespace {
 
 // The batched fit behind bsfit_batch_fit_device (starts null) and
-// bsfit_batch_fit_multistart_device (starts[i] for segment i).
+// bsfit_batch_fit_multistart_device (starts[i] for segment i). warp_rois: the
+// ROIs a warp fits before it ends (BatchArgs::warp_rois; 0: persistent; -1:
+// the per-fit-type caps of batch_fit_capped).
 int batch_fit(const bsfit_segment* segs, const bsfit_starts* starts, int32_t nseg,
-              void* d_scratch, int64_t scratch_bytes, void* stream) {
+              void* d_scratch, int64_t scratch_bytes, void* stream, int warp_rois = 0) {
   if (nseg < 0 || nseg > BSFIT_MAX_SEGMENTS) return BSFIT_E_INVALID;
   if (nseg == 0) return BSFIT_OK;
   if (!segs || !d_scratch || scratch_bytes < bsfit_batch_scratch_bytes(nseg)) return BSFIT_E_INVALID;
@@ -433,6 +435,7 @@ int batch_fit(const bsfit_segment* segs, const bsfit_starts* starts, int32_t nse
     a.next = next;
     a.done = done;
     a.flags = 0;
+    a.warp_rois = warp_rois >= 0 ? warp_rois : (mode == 6 ? 4 : mode == 7 ? 2 : 1);
     for (int j = 0; j < k; ++j) {
       const bsfit_segment& g = segs[order[j]];
       bsfit::BatchSeg& b = a.seg[j];
@@ -461,6 +464,16 @@ int batch_fit(const bsfit_segment* segs, const bsfit_starts* starts, int32_t nse
 }
 
 }  // namespace
+
+namespace bsfit {
+// The serving loop's batched fit: capped, the warps of each fit type's launch
+// end after a few ROIs (3D 4, 4D 2, 5D 1: about 0.1 to 1.5 ms of a warp), so
+// the blocks of a long launch retire while it runs.
+int batch_fit_capped(const bsfit_segment* segs, const bsfit_starts* starts, int32_t nseg,
+                     void* d_scratch, int64_t scratch_bytes, void* stream, bool capped) {
+  return batch_fit(segs, starts, nseg, d_scratch, scratch_bytes, stream, capped ? -1 : 0);
+}
+}  // namespace bsfit
 
 extern "C" {
 

@@ -186,8 +186,17 @@ cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t 
   int64_t grid = (int64_t)sms * blocks_per_sm;
   const int64_t need = (total + rpw * wpb - 1) / (rpw * wpb);
   if (need < grid) grid = need;
+  // A cap on the ROIs per warp (one-ROI kernels only; the two-ROIs-per-warp
+  // variants stay persistent): enough blocks that every ROI is fitted.
+  BatchArgs b = a;
+  if (rpw != 1) b.warp_rois = 0;
+  if (b.warp_rois > 0) {
+    const int64_t cover = (total + (int64_t)b.warp_rois * wpb - 1) / ((int64_t)b.warp_rois * wpb);
+    if (cover > grid) grid = cover;
+    if (grid > 0x7fffffff) return cudaErrorInvalidValue;
+  }
   if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(a);
+  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(b);
   return cudaGetLastError();
 }
 

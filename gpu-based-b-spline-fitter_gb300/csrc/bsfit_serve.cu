@@ -17,6 +17,12 @@
 //    single-start requests at once and fits all their segments in one
 //    persistent launch, each request still copied back and completed on its
 //    own;
+//  - optionally (bsfit_server_set_priority), a launch goes to one of three
+//    streams of its slot by its estimated device time (short, medium, long:
+//    highest priority first), and its warps end after a few ROIs each, so its
+//    blocks retire while the launch runs: a short request (a 3D frame)
+//    submitted while a long one (a 5D frame) runs gets the SMs as the long
+//    launch's blocks retire instead of after the whole launch;
 //  - a host callback at the end of the stream marks the request done with its
 //    completion time, so results are returned per request as soon as they are
 //    ready and the latency (submit to completion) is exact.
@@ -37,6 +43,13 @@
 
 #include "../../include/bsfit.h"
 #include "bsfit_internal.h"
+
+namespace bsfit {
+// The batched fit with per-fit-type caps on the ROIs a warp fits before it ends
+// (bsfit_api.cu).
+int batch_fit_capped(const bsfit_segment* segs, const bsfit_starts* starts, int32_t nseg,
+                     void* d_scratch, int64_t scratch_bytes, void* stream, bool capped);
+}  // namespace bsfit
 
 namespace {
 
@@ -98,6 +111,7 @@ struct Request {
   int64_t bytes = 0;       // arena bytes
   int64_t offset = -1;     // arena offset
   int slot = -1;
+  cudaStream_t stream = nullptr;  // the stream its group was launched on
   int64_t rois = 0;
   Clock::time_point submitted, started;
   std::atomic<int64_t> done_ns{0};  // completion time (ns since epoch of Clock), 0 while running
@@ -133,8 +147,11 @@ struct bsfit_server_s {
   char* arena_base = nullptr;
   Arena arena;
   std::vector<cudaStream_t> streams;
+  // with priorities on: kLevels streams per slot, highest priority first
+  std::vector<cudaStream_t> pstreams;
   std::vector<std::vector<Request*>> slot_req;  // requests running in each slot (empty: free)
   int merge = 1;  // most queued requests fitted by one launch
+  bool priority = false;
   std::deque<Request*> pending;
   std::map<int64_t, Request*> all;  // every request not yet collected
   std::vector<double> latencies_ms;
@@ -153,8 +170,27 @@ namespace {
 // request's uploads, one batched launch over all their segments (the first
 // request's block holds the group's work-queue counters), then every request's
 // result copies and completion callback. Caller holds the mutex.
+constexpr int kLevels = 3;
+
+// Priority level of a group by its estimated device time: ROIs weighted by
+// their fit type's cost relative to a 3D 13 px fit (4D about 6x, 5D about
+// 30x, measured on GB300) and by their pixel count; up to about 1 ms of the
+// GPU is short, up to about 5 ms medium.
+int group_level(const std::vector<Request*>& grp) {
+  double cost = 0.0;
+  for (const Request* r : grp)
+    for (const auto& g : r->segs) {
+      const int ft = bsfit_model_fittype(g.model);
+      const double w = ft == 6 ? 1.0 : ft == 7 ? 6.0 : 30.0;
+      cost += (double)g.nfits * w * (double)(g.roi_size * g.roi_size) / 169.0;
+    }
+  return cost <= 4e4 ? 0 : cost <= 2e5 ? 1 : 2;
+}
+
 int launch_group(bsfit_server_s* s, int slot, const std::vector<Request*>& grp) {
-  cudaStream_t st = s->streams[slot];
+  cudaStream_t st = s->priority ? s->pstreams[slot * kLevels + group_level(grp)]
+                                : s->streams[slot];
+  for (Request* r : grp) r->stream = st;
   std::vector<bsfit_segment> dsegs;
   std::vector<bsfit_starts> starts;
   cudaError_t e = cudaSuccess;
@@ -186,10 +222,8 @@ int launch_group(bsfit_server_s* s, int slot, const std::vector<Request*>& grp) 
   if (e != cudaSuccess) return cuda_status_s(e);
   void* scratch = s->arena_base + grp[0]->offset;
   const int64_t sb = bsfit_batch_scratch_bytes((int32_t)dsegs.size());
-  int stt = starts.empty()
-                ? bsfit_batch_fit_device(dsegs.data(), (int32_t)dsegs.size(), scratch, sb, st)
-                : bsfit_batch_fit_multistart_device(dsegs.data(), starts.data(),
-                                                    (int32_t)dsegs.size(), scratch, sb, st);
+  int stt = bsfit::batch_fit_capped(dsegs.data(), starts.empty() ? nullptr : starts.data(),
+                                    (int32_t)dsegs.size(), scratch, sb, st, s->priority);
   if (stt != BSFIT_OK) return stt;
   size_t k = 0;
   for (Request* r : grp) {
@@ -243,7 +277,7 @@ void admit(bsfit_server_s* s) {
     int st = launch_group(s, slot, grp);
     if (st != BSFIT_OK) {
       // The group failed to launch: complete its requests with the error.
-      cudaStreamSynchronize(s->streams[slot]);
+      cudaStreamSynchronize(grp[0]->stream);
       for (Request* r : grp) {
         r->status = st;
         r->done_ns.store(Clock::now().time_since_epoch().count());
@@ -300,8 +334,19 @@ int bsfit_server_create(int32_t max_inflight, int64_t arena_bytes, bsfit_server*
   s->slot_req.assign(max_inflight, {});
   for (int i = 0; i < max_inflight && e == cudaSuccess; ++i)
     e = cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking);
+  // the priority streams: levels spread over the device's priority range
+  int least = 0, greatest = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  s->pstreams.resize((size_t)max_inflight * kLevels, nullptr);
+  for (int i = 0; i < max_inflight * kLevels && e == cudaSuccess; ++i) {
+    const int lv = i % kLevels;  // 0: greatest priority
+    const int pr = greatest + (least - greatest) * lv / (kLevels - 1);
+    e = cudaStreamCreateWithPriority(&s->pstreams[i], cudaStreamNonBlocking, pr);
+  }
   if (e != cudaSuccess) {
     for (auto st : s->streams)
+      if (st) cudaStreamDestroy(st);
+    for (auto st : s->pstreams)
       if (st) cudaStreamDestroy(st);
     cudaFree(s->arena_base);
     delete s;
@@ -319,10 +364,19 @@ int bsfit_server_set_merge(bsfit_server s, int32_t max_requests_per_launch) {
   return BSFIT_OK;
 }
 
+int bsfit_server_set_priority(bsfit_server s, int32_t enable) {
+  if (!s) return BSFIT_E_INVALID;
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->priority = enable != 0;
+  return BSFIT_OK;
+}
+
 int bsfit_server_destroy(bsfit_server s) {
   if (!s) return BSFIT_E_INVALID;
   for (auto st : s->streams) cudaStreamSynchronize(st);
+  for (auto st : s->pstreams) cudaStreamSynchronize(st);
   for (auto st : s->streams) cudaStreamDestroy(st);
+  for (auto st : s->pstreams) cudaStreamDestroy(st);
   cudaFree(s->arena_base);
   for (auto& kv : s->all) delete kv.second;
   delete s;

@@ -308,6 +308,14 @@ int bsfit_server_destroy(bsfit_server server);
  * on its own. 1 (the default) launches every request alone. Results do not
  * depend on the setting. */
 int bsfit_server_set_merge(bsfit_server server, int32_t max_requests_per_launch);
+/* Priority launches (no counterpart in the reference): with enable set, each
+ * launch goes to one of three streams of its slot by its estimated device time
+ * (short ones, like a 3D frame, at the device's highest stream priority), and
+ * its warps end after a few ROIs each so that its blocks retire while it runs:
+ * a short request submitted while a long one (a 5D frame) runs starts on the
+ * SMs its blocks free instead of after the long launch. Off by default.
+ * Results do not depend on the setting. */
+int bsfit_server_set_priority(bsfit_server server, int32_t enable);
 /* As bsfit_server_submit, with per-segment starts (bsfit_starts, see
  * bsfit_batch_fit_multistart_device): the request's fits run the callers'
  * multi-start inside the batched launch. */

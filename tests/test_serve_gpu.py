@@ -177,3 +177,48 @@ def test_serving_merged_launches_match_plain(bsfit_mod):
     with pytest.raises(bsfit_mod.BsfitError):
         bsfit_mod.Server(max_inflight=1, arena_bytes=1 << 20, merge=0)
     srv.close()
+
+
+@pytest.mark.parametrize("merge", [1, 4])
+def test_serving_priority_launches_match_plain(bsfit_mod, merge):
+    """With priority launches on (bsfit_server_set_priority: streams of three
+    priorities by estimated device time, warps that end after a few ROIs),
+    requests of mixed models, submitted together so that short ones run beside
+    long ones, give each request the plain call's results bit for bit, and a
+    multi-start request the fused multi-start call's. The two large frames (a
+    3D frame of 20,000 ROIs, a 5D frame of 2,000) outnumber the warps that can
+    be resident times their caps, so their launches retire and start blocks."""
+    from bsfit import workloads as W
+    frames = _frames() * 2 + [("3d", W.workload_3d(20000, s=11, stream=812)),
+                              ("5d", W.workload_5d(2000, stream=813))]
+    models = {}
+    for kind, w in frames:
+        if kind not in models:
+            models[kind] = bsfit_mod.Model(w.fittype, w.coeff, coeff3=w.coeff3, init_p=w.init_p)
+    srv = bsfit_mod.Server(max_inflight=3, arena_bytes=96 << 20, merge=merge, priority=True)
+    ids = [srv.submit([(models[kind], w.rois, w.iterations)]) for kind, w in frames]
+    w4 = frames[4][1]
+    z, wv = float(w4.init_p[0]), float(w4.init_p[1])
+    st4 = np.array([[1.2 * z, wv], [z, wv]], np.float32)
+    ms = srv.submit([(models["4d"], w4.rois, w4.iterations)], starts=[st4])
+    results = {rid: srv.wait(rid, timeout=120.0) for rid in ids + [ms]}
+    st = srv.stats()
+    assert st["completed"] == len(results) and st["in_flight"] == 0 and st["queued"] == 0
+    for rid, (kind, w) in zip(ids, frames):
+        kw = {}
+        if w.init_p is not None:
+            kw["initP"] = w.init_p
+        if w.coeff3 is not None:
+            kw["coeff3"] = w.coeff3
+        P, C, L = bsfit_mod.GPUmleFit_LM_multiD(w.rois, w.fittype, w.iterations, w.coeff, **kw)
+        Ps, Cs, Ls = results[rid][0]
+        assert np.array_equal(Ps, P, equal_nan=True), kind
+        assert np.array_equal(Cs, C, equal_nan=True), kind
+        assert np.array_equal(Ls, L, equal_nan=True), kind
+    import torch
+    P, C, L = (x.cpu().numpy() for x in models["4d"].fit_multistart_torch(
+        torch.from_numpy(w4.rois).cuda(), w4.iterations, st4))
+    Ps, Cs, Ls = results[ms][0]
+    assert np.array_equal(Ps, P.T, equal_nan=True)
+    assert np.array_equal(Ls, L, equal_nan=True)
+    srv.close()

@@ -166,10 +166,6 @@ struct bsfit_server_s {
 
 namespace {
 
-// Enqueue an admitted group of requests on their slot's stream: every
-// request's uploads, one batched launch over all their segments (the first
-// request's block holds the group's work-queue counters), then every request's
-// result copies and completion callback. Caller holds the mutex.
 constexpr int kLevels = 3;
 
 // Priority level of a group by its estimated device time: ROIs weighted by
@@ -187,6 +183,11 @@ int group_level(const std::vector<Request*>& grp) {
   return cost <= 4e4 ? 0 : cost <= 2e5 ? 1 : 2;
 }
 
+// Enqueue an admitted group of requests on a stream of its slot (with
+// priorities on, the stream of the group's level): every request's uploads,
+// one batched launch over all their segments (the first request's block holds
+// the group's work-queue counters), then every request's result copies and
+// completion callback. Caller holds the mutex.
 int launch_group(bsfit_server_s* s, int slot, const std::vector<Request*>& grp) {
   cudaStream_t st = s->priority ? s->pstreams[slot * kLevels + group_level(grp)]
                                 : s->streams[slot];

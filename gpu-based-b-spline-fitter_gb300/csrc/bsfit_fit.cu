@@ -163,16 +163,32 @@ cudaError_t pick_launch_wpb(const void* kern, int per_warp, int force_wpb, int* 
 cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t stream) {
   if (a.nseg <= 0) return cudaSuccess;
   void (*kern)(const BatchArgs) = nullptr;
-  if (mode == 6 && !multi) kern = batch_kernel<6>;
-  else if (mode == 7) kern = multi ? batch_kernel<7, true> : batch_kernel<7>;
-  else if (mode == 8) kern = multi ? batch_kernel<8, true> : batch_kernel<8>;
-  else return cudaErrorInvalidValue;
-  // the autotuner's configuration for the largest ROI size of the batch
+  const bool cap = a.warp_rois > 0;
+  constexpr int M6 = BSFIT_MINBLOCKS(6), M7 = BSFIT_MINBLOCKS(7), M8 = BSFIT_MINBLOCKS(8);
+  if (cap) {
+    // the capped form of the default kernel (the serving loop's priority launches)
+    if (mode == 6 && !multi) kern = batch_kernel<6, false, M6, 0, true>;
+    else if (mode == 7) kern = multi ? batch_kernel<7, true, M7, 0, true> : batch_kernel<7, false, M7, 0, true>;
+    else if (mode == 8) kern = multi ? batch_kernel<8, true, M8, 0, true> : batch_kernel<8, false, M8, 0, true>;
+    else return cudaErrorInvalidValue;
+  } else if (mode == 6 && !multi) {
+    kern = batch_kernel<6>;
+  } else if (mode == 7) {
+    kern = multi ? batch_kernel<7, true> : batch_kernel<7>;
+  } else if (mode == 8) {
+    kern = multi ? batch_kernel<8, true> : batch_kernel<8>;
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  // the autotuner's configuration for the largest ROI size of the batch (the
+  // capped form keeps the default kernel and takes the tuner's warps per block)
   TuneConfig tc{0, 0};
   int dev = 0;
   if (!multi && cudaGetDevice(&dev) == cudaSuccess && tune_lookup(mode, a.s_max, dev, &tc) &&
-      tc.variant > 0)
-    kern = batch_variant(mode, tc.variant);
+      tc.variant > 0) {
+    if (cap) tc.variant = 0;
+    else kern = batch_variant(mode, tc.variant);
+  }
   if (!kern) return cudaErrorInvalidValue;
   const int rpw = tune_rois_per_warp(mode, tc.variant);
   const int per_warp = tune_warp_floats(mode, tc.variant, a.s_max, false) * 4;
@@ -186,17 +202,14 @@ cudaError_t launch_batch(const BatchArgs& a, int mode, bool multi, cudaStream_t 
   int64_t grid = (int64_t)sms * blocks_per_sm;
   const int64_t need = (total + rpw * wpb - 1) / (rpw * wpb);
   if (need < grid) grid = need;
-  // A cap on the ROIs per warp (one-ROI kernels only; the two-ROIs-per-warp
-  // variants stay persistent): enough blocks that every ROI is fitted.
-  BatchArgs b = a;
-  if (rpw != 1) b.warp_rois = 0;
-  if (b.warp_rois > 0) {
-    const int64_t cover = (total + (int64_t)b.warp_rois * wpb - 1) / ((int64_t)b.warp_rois * wpb);
+  // capped: enough blocks that every ROI is fitted
+  if (cap) {
+    const int64_t cover = (total + (int64_t)a.warp_rois * wpb - 1) / ((int64_t)a.warp_rois * wpb);
     if (cover > grid) grid = cover;
     if (grid > 0x7fffffff) return cudaErrorInvalidValue;
   }
   if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(b);
+  kern<<<(unsigned)grid, 32 * wpb, smem, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -1681,11 +1681,12 @@ __global__ void __launch_bounds__(128, MINB) fit_kernel(FitArgs a) {
 // fits them, and counts them done. The warp's shared memory is laid out for
 // the largest ROI of the batch. MULTI: every ROI is fitted from its segment's
 // starts and the best log-likelihood kept (fit_and_store), in a separate
-// instantiation so the single-start kernel carries no start loop. With
-// a.warp_rois set, a warp stops after that many ROIs (the grid then covers
-// every ROI, and blocks retire as they finish).
-
-template <int MODE, bool MULTI = false, int MINB = BSFIT_MINBLOCKS(MODE), int STG = 0>
+// instantiation so the single-start kernel carries no start loop. CAP: the
+// serving loop's capped form, where a warp stops after a.warp_rois ROIs (the
+// grid then covers every ROI, and blocks retire as they finish); a separate
+// instantiation, so the persistent kernels carry no counter.
+template <int MODE, bool MULTI = false, int MINB = BSFIT_MINBLOCKS(MODE), int STG = 0,
+          bool CAP = false>
 __global__ void __launch_bounds__(128, MINB) batch_kernel(const __grid_constant__ BatchArgs a) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
@@ -1693,8 +1694,8 @@ __global__ void __launch_bounds__(128, MINB) batch_kernel(const __grid_constant_
   const int wib = threadIdx.x >> 5;
   float* ws = smem + wib * make_layout(MODE, a.s_max, false, STG).total();
   int seg = 0;
-  int fitted = 0;
-  while (seg < a.nseg && (a.warp_rois == 0 || fitted < a.warp_rois)) {
+  int fitted = 0;  // ROIs this warp has fitted (CAP)
+  while (seg < a.nseg && (!CAP || fitted < a.warp_rois)) {
     const BatchSeg& g = a.seg[seg];
     unsigned long long i = 0;
     if (lane == 0) i = atomicAdd(&a.next[g.slot], 1ull);
@@ -1734,7 +1735,7 @@ __global__ void __launch_bounds__(128, MINB) batch_kernel(const __grid_constant_
     }
     fit_and_store<MODE, MULTI, false, STG>(fa, make_layout(MODE, g.s, false, STG), ws, lane, (int64_t)i);
     if (lane == 0) atomicAdd(&a.done[g.slot], 1ull);
-    ++fitted;
+    if constexpr (CAP) ++fitted;
   }
 }
 

@@ -129,10 +129,11 @@ struct BatchArgs {
   int nseg;
   int s_max;
   int flags;
-  // ROIs a warp of the one-ROI batched kernel fits before it ends (0: until
-  // the queue is empty). With a cap the grid covers every ROI and blocks retire
-  // as they finish, so the work of a launch on a higher-priority stream starts
-  // as soon as a block's resources free up instead of after the whole launch.
+  // ROIs a warp fits before it ends (0: until the queue is empty; > 0: the
+  // capped form of the default kernel). With a cap the grid covers every ROI
+  // and blocks retire as they finish, so the work of a launch on a
+  // higher-priority stream starts as soon as a block's resources free up
+  // instead of after the whole launch.
   int warp_rois;
   // Work queue in caller-provided device scratch: next[i] is the next
   // unclaimed ROI of segment i, done[i] counts its finished ROIs.

@@ -465,6 +465,13 @@ def bench_serving(args, dev, seed=11):
     psat_s, _ = run_stream(srv, frames, [0] * len(frames))
     prio = {"fits_per_s": n_rois / psat_s, "frame10k_mixed": mixed10k(srv, fm_sat_s)[1]}
     srv.close()
+    # both: priority launches and merged admission of requests of one level
+    srv = bsfit.Server(max_inflight=4, arena_bytes=4 << 30, merge=4, priority=True)
+    run_stream(srv, frames[:4], [0] * 4)  # warm-up
+    bsat_s, _ = run_stream(srv, frames, [0] * len(frames))
+    prio["merged"] = {"merge": 4, "fits_per_s": n_rois / bsat_s,
+                      "frame10k_mixed": mixed10k(srv, fm_sat_s)[1]}
+    srv.close()
     # plain per-call form
     t0 = time.perf_counter()
     for kind, w, r in frames:

@@ -168,18 +168,18 @@ namespace {
 
 constexpr int kLevels = 3;
 
-// Priority level of a group by its estimated device time: ROIs weighted by
+// Priority level of a request by its estimated device time: ROIs weighted by
 // their fit type's cost relative to a 3D 13 px fit (4D about 6x, 5D about
 // 30x, measured on GB300) and by their pixel count; up to about 1 ms of the
-// GPU is short, up to about 5 ms medium.
-int group_level(const std::vector<Request*>& grp) {
+// GPU is short, up to about 5 ms medium. A merged group takes its first
+// request's level (admission merges requests of one level only).
+int request_level(const Request* r) {
   double cost = 0.0;
-  for (const Request* r : grp)
-    for (const auto& g : r->segs) {
-      const int ft = bsfit_model_fittype(g.model);
-      const double w = ft == 6 ? 1.0 : ft == 7 ? 6.0 : 30.0;
-      cost += (double)g.nfits * w * (double)(g.roi_size * g.roi_size) / 169.0;
-    }
+  for (const auto& g : r->segs) {
+    const int ft = bsfit_model_fittype(g.model);
+    const double w = ft == 6 ? 1.0 : ft == 7 ? 6.0 : 30.0;
+    cost += (double)g.nfits * w * (double)(g.roi_size * g.roi_size) / 169.0;
+  }
   return cost <= 4e4 ? 0 : cost <= 2e5 ? 1 : 2;
 }
 
@@ -189,7 +189,7 @@ int group_level(const std::vector<Request*>& grp) {
 // the group's work-queue counters), then every request's result copies and
 // completion callback. Caller holds the mutex.
 int launch_group(bsfit_server_s* s, int slot, const std::vector<Request*>& grp) {
-  cudaStream_t st = s->priority ? s->pstreams[slot * kLevels + group_level(grp)]
+  cudaStream_t st = s->priority ? s->pstreams[slot * kLevels + request_level(grp[0])]
                                 : s->streams[slot];
   for (Request* r : grp) r->stream = st;
   std::vector<bsfit_segment> dsegs;
@@ -262,7 +262,8 @@ void admit(bsfit_server_s* s) {
     while (!s->pending.empty() && (int)grp.size() < s->merge) {
       Request* r = s->pending.front();
       if (!grp.empty() && (!r->starts.empty() || !grp[0]->starts.empty() ||
-                           nseg + r->segs.size() > (size_t)BSFIT_MAX_SEGMENTS))
+                           nseg + r->segs.size() > (size_t)BSFIT_MAX_SEGMENTS ||
+                           (s->priority && request_level(r) != request_level(grp[0]))))
         break;
       int64_t off = s->arena.alloc(r->bytes);
       if (off < 0) break;  // wait for memory to free up

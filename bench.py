@@ -670,10 +670,11 @@ def bench_gpu(args):
         for g, p, o in zip(groups, pinned, host_out):
             bsfit.GPUmleFit_LM_multiD(p, 6, g.iterations, g.coeff, out=o)
     barrier()
-    # up to 20 steps (about 0.6 s) so that one host-side stall (a shared host:
-    # one step in ten once took 53 ms against 29.6 ms) moves the mean little;
-    # each step's time is kept for the spread reported beside it
-    e2e_steps = max(1, min(args.steps, 20))
+    # three times the timed steps, up to 60 (about 1.8 s), so that a host-side
+    # stall (a shared host: about one step in 20 to 30 takes 41-64 ms against
+    # 29.2 ms) moves the mean little; each step's time is kept for the spread
+    # reported beside it
+    e2e_steps = max(1, min(3 * args.steps, 60))
     e2e_ms = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
